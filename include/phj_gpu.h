@@ -1,0 +1,259 @@
+/*
+ * phj_gpu.h -- C ABI of the GB300 (sm_103a) hash-join hot path.
+ *
+ * The reference (harikrishnan94/phj-bench) has no FFI: its boundary is three
+ * C++ entry points over host BlockStreams,
+ *     runCHJ    (src/CHJ.h:31)
+ *     runPHJ    (src/PHJ.h:31)      -- the "phj-pure" scheme
+ *     runPhjBep (src/PHJBep.h:97-98) -- the "phj" (best-effort partitioning) scheme
+ * and their result structs.  This header is the C form of that boundary:
+ * plain pointers and sizes, status codes instead of exceptions, one device,
+ * one CUDA stream per context.  Each declaration names the reference
+ * interface it replaces.  phj-bench_gb300/host/phj_gpu.hpp layers the
+ * reference's C++ signatures on top of it.
+ *
+ * Threading: a context is used by one host thread at a time (the reference's
+ * run* functions are likewise blocking calls from one thread).  Every run
+ * call is blocking: it returns when the join is complete on the device.
+ */
+#ifndef PHJ_GPU_H
+#define PHJ_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PHJ_GPU_ABI_VERSION 1u
+#define PHJ_MAX_PAYLOADS 8u /* payload columns per side */
+
+/* Error codes.  The reference throws std::invalid_argument / std::bad_alloc
+ * (src/RadixPartition.cpp:554-560); across a C ABI they become codes, with
+ * the message available from phj_last_error(). */
+typedef enum phj_status {
+    PHJ_OK = 0,
+    PHJ_ERR_INVALID_ARGUMENT = 1,
+    PHJ_ERR_CUDA = 2,
+    PHJ_ERR_OUT_OF_MEMORY = 3,
+    PHJ_ERR_UNSUPPORTED = 4,
+    PHJ_ERR_DEVICE_TIMEOUT = 5, /* a bounded device wait gave up */
+    PHJ_ERR_NO_DEVICE = 6,
+    PHJ_ERR_CAPACITY = 7        /* caller-provided capacity too small */
+} phj_status;
+
+/* PayloadType, src/Types.h:23-30 (same codes, same widths 1/2/4/8/16). */
+typedef enum phj_payload_type {
+    PHJ_U8 = 0,
+    PHJ_U16 = 1,
+    PHJ_U32 = 2,
+    PHJ_U64 = 3,
+    PHJ_U128 = 4
+} phj_payload_type;
+
+/* RowRefCell, src/Types.h:95-104: 8 bytes; empty <=> block_no == 0xFFFFFFFF. */
+typedef struct phj_row_ref {
+    uint32_t block_no;
+    uint32_t row_no;
+} phj_row_ref;
+
+/* JoinHashTable::Cell, src/HashTable.h:33-38: 16 bytes (key, RowRefCell). */
+typedef struct phj_ht_cell {
+    uint64_t key;
+    phj_row_ref ref;
+} phj_ht_cell;
+
+/* PayloadSchema, src/Types.h:69-80. */
+typedef struct phj_schema {
+    uint32_t n_payloads;
+    uint8_t types[PHJ_MAX_PAYLOADS];
+} phj_schema;
+
+typedef enum phj_location { PHJ_HOST = 0, PHJ_DEVICE = 1 } phj_location;
+
+/* BlockStream, src/Block.h:157-162, with its blocks laid end to end: one key
+ * column and one column per payload, `total_rows` long, split into
+ * `n_blocks` blocks of `block_rows[i]` rows (block_rows == NULL: one block).
+ * Block numbers are the build side's RowRefCell.block_no for CHJ. */
+typedef struct phj_block_stream {
+    phj_schema schema;
+    uint64_t total_rows;
+    uint32_t n_blocks;
+    const uint32_t *block_rows;               /* host array of n_blocks, or NULL */
+    const uint64_t *keys;
+    const void *payloads[PHJ_MAX_PAYLOADS];   /* column c: total_rows * width(c) bytes */
+    int32_t location;                         /* phj_location of keys/payloads */
+} phj_block_stream;
+
+/* PhaseTiming, src/JoinOutput.h:79-83 (device time from CUDA events). */
+typedef struct phj_phase_timing {
+    double wall_ms;
+    double ns_per_row;
+} phj_phase_timing;
+
+/* ChjResult minus the output, src/CHJ.h:12-19. */
+typedef struct phj_chj_result {
+    phj_phase_timing build;
+    phj_phase_timing probe;
+    double e2e_wall_ms;
+    uint64_t peak_mem_bytes; /* peak device bytes held by the run */
+} phj_chj_result;
+
+/* PhjResult minus the output, src/PHJ.h:13-22. */
+typedef struct phj_phj_result {
+    phj_phase_timing build_shuffle;
+    phj_phase_timing build;
+    phj_phase_timing probe_shuffle;
+    phj_phase_timing probe;
+    double e2e_wall_ms;
+    uint64_t peak_mem_bytes;
+} phj_phj_result;
+
+/* PhjBepResult minus the output, src/PHJBep.h:13-39. */
+typedef struct phj_bep_result {
+    phj_phase_timing build_shuffle;
+    phj_phase_timing build;
+    phj_phase_timing probe_shuffle;
+    phj_phase_timing probe;
+    phj_phase_timing eviction_overhead;
+    double e2e_wall_ms;
+    uint64_t peak_mem_bytes;
+    uint64_t bep_budget_mib;
+    uint64_t bep_evictions;
+    uint64_t bep_refinements;
+    uint64_t bep_peak_bytes;
+    uint64_t bep_build_skip_retries;
+} phj_bep_result;
+
+typedef struct phj_ctx phj_ctx;       /* device, stream, memory pool, timers */
+typedef struct phj_table phj_table;   /* a device-resident BlockStream */
+typedef struct phj_output phj_output; /* a device-resident JoinOutput (src/JoinOutput.h:55-70) */
+
+/* ---- context ---------------------------------------------------------- */
+
+/* Opens `device`, creates the context's stream and stream-ordered pool. */
+phj_status phj_ctx_create(int device, phj_ctx **out);
+void phj_ctx_destroy(phj_ctx *ctx);
+/* Message of the last failing call on this context ("" if none). */
+const char *phj_last_error(const phj_ctx *ctx);
+uint32_t phj_abi_version(void);
+/* The context's CUDA stream (a cudaStream_t). */
+void *phj_ctx_stream(phj_ctx *ctx);
+/* Integer options of a context:
+ *   "probe_materialize": -1 auto (default), 0 never, 1 always -- whether the
+ *        partitioned schemes write the probe side's first radix pass to
+ *        memory or probe the input order directly against the leaf tables;
+ *   "time_kernels": 1 (default) records CUDA events around each kernel. */
+phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);
+
+/* ---- radix configuration: CLI.cpp:376-408 ------------------------------ */
+
+/* Resolves --partitions/--passes (or an explicit --partition-bits-per-pass
+ * list when n_bits_override > 0) into per-pass bits exactly as the
+ * reference CLI does: bits split evenly, the extra bits to the earlier
+ * passes; total bits in [1, 32].  `out_bits` must hold 32 entries. */
+phj_status phj_resolve_radix(uint64_t partitions, uint32_t passes, const uint8_t *bits_override,
+                             uint32_t n_bits_override, uint8_t *out_bits, uint32_t *out_n_passes);
+
+/* ---- input streams -------------------------------------------------------- */
+
+/* Copies a host BlockStream into device memory (replaces nothing in the
+ * reference, whose streams are host-resident; needed because the schemes
+ * below read device memory). */
+phj_status phj_table_upload(phj_ctx *ctx, const phj_block_stream *host_stream, phj_table **out);
+/* Wraps device columns without copying; the caller keeps them alive. */
+phj_status phj_table_wrap_device(phj_ctx *ctx, const phj_block_stream *device_stream, phj_table **out);
+/* Fills device columns with a seeded synthetic workload (see phj_gen_spec). */
+typedef struct phj_gen_spec {
+    uint32_t kind;        /* 0 build, unique keys K(i)                      */
+                          /* 1 build, keys = permutation of 1..rows           */
+                          /* 2 build, multi-match: geometric multiplicities   */
+                          /* 3 probe, uniform over [1, key_domain]            */
+                          /* 4 probe, K(uniform(domain)) w.p. match_permille/1000, else non-matching */
+                          /* 5 probe, Zipf(theta) ranks through a permutation of K(0..domain-1) */
+    uint64_t rows;
+    uint64_t seed;
+    uint64_t key_seed;    /* seed of the K(i) key stream shared by both sides */
+    uint64_t domain;      /* kind 3: max key; kind 4/5: number of build keys K(0..domain-1); kind 2: distinct-key cap */
+    uint32_t match_permille;
+    double theta;         /* kind 5 */
+    phj_schema schema;
+    uint32_t block_rows;  /* block size of the generated stream (10000 in the reference) */
+} phj_gen_spec;
+phj_status phj_table_generate(phj_ctx *ctx, const phj_gen_spec *spec, phj_table **out);
+/* Copies a device table back to host columns (keys, then payload columns). */
+phj_status phj_table_download(phj_ctx *ctx, const phj_table *t, uint64_t *keys, void *const *payloads);
+uint64_t phj_table_rows(const phj_table *t);
+/* Distinct keys of a table generated with kind 0 or 2 (0 otherwise). */
+uint64_t phj_table_gen_distinct(const phj_table *t);
+void phj_table_free(phj_ctx *ctx, phj_table *t);
+
+/* ---- the three schemes ---------------------------------------------------- */
+
+/* runCHJ (src/CHJ.h:31, src/CHJ.cpp:49-152): one global device table of
+ * 16-byte cells namespaced by the top 8 hash bits, 128-bit CAS inserts, then
+ * an unpartitioned probe.  `threads` of the reference has no device meaning. */
+phj_status phj_run_chj(phj_ctx *ctx, const phj_table *build, const phj_table *probe, phj_output **out,
+                       phj_chj_result *result);
+
+/* runPHJ (src/PHJ.h:31, src/PHJ.cpp:19-150): radix shuffle of both sides
+ * over `pass_bits` (n_passes passes, total bits in [1, 24] on the device),
+ * per-leaf tables, probe with output projection. */
+phj_status phj_run_phj_pure(phj_ctx *ctx, const phj_table *build, const phj_table *probe, const uint8_t *pass_bits,
+                            uint32_t n_passes, phj_output **out, phj_phj_result *result);
+
+/* runPhjBep (src/PHJBep.h:97-98, src/PHJBep.cpp:113-790): bounded probe-side
+ * buffering, refinement and eviction with lazily built leaf tables inside a
+ * persistent kernel.  `bep_budget_mib` is the probe-buffer budget of one
+ * worker (a persistent CTA group); `workers` = number of CTA groups (0 =
+ * one per SM). */
+phj_status phj_run_phj_bep(phj_ctx *ctx, const phj_table *build, const phj_table *probe, const uint8_t *pass_bits,
+                           uint32_t n_passes, uint64_t bep_budget_mib, uint32_t workers, phj_output **out,
+                           phj_bep_result *result);
+
+/* ---- output --------------------------------------------------------------- */
+
+uint64_t phj_output_rows(const phj_output *out);
+/* Device column pointers: key column, build (left) columns, probe (right)
+ * columns; the schemas are the build and probe schemas (OutputBlock,
+ * src/JoinOutput.h:18-42). */
+phj_status phj_output_device_columns(const phj_output *out, const uint64_t **keys, const void **left,
+                                     const void **right);
+/* Copies the output to host columns sized phj_output_rows() rows. */
+phj_status phj_output_download(phj_ctx *ctx, const phj_output *out, uint64_t *keys, void *const *left,
+                               void *const *right);
+/* Order-independent fingerprint of the output multiset computed on the
+ * device: fp[0] rows, fp[1], fp[2] sums of two per-row hashes (the oracle
+ * computes the same for the reference join). */
+phj_status phj_output_fingerprint(phj_ctx *ctx, const phj_output *out, uint64_t fp[3]);
+void phj_output_free(phj_ctx *ctx, phj_output *out);
+
+/* ---- measurement hooks ------------------------------------------------------ */
+
+/* Per-kernel device times of the last run (CUDA events on the context's
+ * stream).  Fills up to `cap` entries; returns the number recorded. */
+typedef struct phj_kernel_time {
+    char name[32];
+    double ms;
+    uint64_t rows;   /* rows the launch processed */
+    uint64_t bytes;  /* algorithmic bytes the launch read+wrote */
+} phj_kernel_time;
+uint32_t phj_last_kernel_times(const phj_ctx *ctx, phj_kernel_time *out, uint32_t cap);
+/* Number of this library's kernel launches issued since the context was
+ * created. */
+uint64_t phj_launch_count(const phj_ctx *ctx);
+
+/* Pinned host memory (for host buffers of the end-to-end path). */
+phj_status phj_host_alloc(phj_ctx *ctx, size_t bytes, void **out);
+void phj_host_free(phj_ctx *ctx, void *p);
+
+/* Writes `bytes` bytes over a scratch buffer larger than L2 so the next
+ * timed run starts with a cold cache. */
+phj_status phj_flush_l2(phj_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PHJ_GPU_H */

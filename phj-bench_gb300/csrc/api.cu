@@ -1,0 +1,931 @@
+// api.cu -- the C ABI (include/phj_gpu.h): context, streams of rows on the
+// device, the three join schemes, outputs, and measurement hooks.
+#include "internal.h"
+
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace phjg
+{
+// ---------------------------------------------------------------------------
+// errors, launches, timing
+// ---------------------------------------------------------------------------
+void cuda_check(cudaError_t e, const char * what, const char * file, int line)
+{
+    if (e == cudaSuccess)
+        return;
+    char buf[512];
+    std::snprintf(buf, sizeof(buf), "%s failed: %s (%s:%d)", what, cudaGetErrorString(e), file, line);
+    throw Error(e == cudaErrorMemoryAllocation ? PHJ_ERR_OUT_OF_MEMORY : PHJ_ERR_CUDA, buf);
+}
+
+void after_launch(phj_ctx * ctx, const char * name, const char * file, int line)
+{
+    ++ctx->launches;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+    {
+        char buf[512];
+        std::snprintf(buf, sizeof(buf), "launch of %s failed: %s (%s:%d)", name, cudaGetErrorString(e), file, line);
+        throw Error(PHJ_ERR_CUDA, buf);
+    }
+}
+
+cudaEvent_t take_event(phj_ctx * ctx)
+{
+    if (ctx->event_next == ctx->event_pool.size())
+    {
+        cudaEvent_t e;
+        PHJ_CUDA(cudaEventCreate(&e));
+        ctx->event_pool.push_back(e);
+    }
+    return ctx->event_pool[ctx->event_next++];
+}
+
+void begin_run(phj_ctx * ctx)
+{
+    ctx->records.clear();
+    ctx->event_next = 0;
+    reset_accounting(ctx);
+}
+
+KTimer::KTimer(phj_ctx * c, const char * name, uint64_t rows, uint64_t bytes)
+    : ctx(c)
+{
+    if (!ctx->time_kernels)
+        return;
+    KernelRecord r;
+    r.name = name;
+    r.rows = rows;
+    r.bytes = bytes;
+    r.start = take_event(ctx);
+    r.stop = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(r.start, ctx->stream));
+    ctx->records.push_back(r);
+    idx = (int)ctx->records.size() - 1;
+}
+
+KTimer::~KTimer()
+{
+    if (idx >= 0)
+        cudaEventRecord(ctx->records[idx].stop, ctx->stream);
+}
+
+float event_ms(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    PHJ_CUDA(cudaEventElapsedTime(&ms, a, b));
+    return ms;
+}
+
+// ---------------------------------------------------------------------------
+// allocation: the context's stream-ordered pool, with per-run accounting
+// ---------------------------------------------------------------------------
+void * dalloc(phj_ctx * ctx, size_t bytes)
+{
+    void * p = nullptr;
+    const size_t rounded = (bytes + 255) & ~size_t(255);
+    const cudaError_t e = cudaMallocFromPoolAsync(&p, rounded, ctx->pool, ctx->stream);
+    if (e != cudaSuccess)
+    {
+        cudaGetLastError();
+        char buf[160];
+        std::snprintf(buf, sizeof(buf), "device allocation of %zu bytes failed: %s", rounded, cudaGetErrorString(e));
+        throw Error(PHJ_ERR_OUT_OF_MEMORY, buf);
+    }
+    ctx->live.emplace_back(p, rounded);
+    ctx->cur_bytes += rounded;
+    ctx->peak_bytes = std::max(ctx->peak_bytes, ctx->cur_bytes);
+    return p;
+}
+
+void dfree(phj_ctx * ctx, void * p)
+{
+    if (!p)
+        return;
+    for (size_t i = ctx->live.size(); i-- > 0;)
+        if (ctx->live[i].first == p)
+        {
+            ctx->cur_bytes -= ctx->live[i].second;
+            ctx->live[i] = ctx->live.back();
+            ctx->live.pop_back();
+            break;
+        }
+    cudaFreeAsync(p, ctx->stream);
+}
+
+void reset_accounting(phj_ctx * ctx)
+{
+    ctx->peak_bytes = ctx->cur_bytes;
+}
+
+// ---------------------------------------------------------------------------
+// columns
+// ---------------------------------------------------------------------------
+Cols cols_of(const phj_table & t)
+{
+    Cols c{};
+    c.keys = t.keys;
+    c.n = t.schema.n_payloads;
+    for (uint32_t i = 0; i < c.n; ++i)
+    {
+        c.col[i] = t.cols[i];
+        c.width[i] = (uint8_t)payload_width(t.schema.types[i]);
+    }
+    return c;
+}
+
+Cols alloc_cols_like(Scratch & s, const phj_schema & schema, uint64_t rows)
+{
+    Cols c{};
+    c.keys = s.get<uint64_t>(rows);
+    c.n = schema.n_payloads;
+    for (uint32_t i = 0; i < c.n; ++i)
+    {
+        c.width[i] = (uint8_t)payload_width(schema.types[i]);
+        c.col[i] = s.get<uint8_t>(rows * c.width[i]);
+    }
+    return c;
+}
+
+uint32_t max_width(const Cols & c)
+{
+    uint32_t w = 0;
+    for (uint32_t i = 0; i < c.n; ++i)
+        w = std::max<uint32_t>(w, c.width[i]);
+    return w;
+}
+
+namespace
+{
+template <class F>
+phj_status guard(phj_ctx * ctx, F && f)
+{
+    try
+    {
+        f();
+        if (ctx)
+            ctx->last_error.clear();
+        return PHJ_OK;
+    }
+    catch (const Error & e)
+    {
+        if (ctx)
+            ctx->last_error = e.what();
+        return e.status;
+    }
+    catch (const std::bad_alloc &)
+    {
+        if (ctx)
+            ctx->last_error = "host allocation failed";
+        return PHJ_ERR_OUT_OF_MEMORY;
+    }
+    catch (const std::exception & e)
+    {
+        if (ctx)
+            ctx->last_error = e.what();
+        return PHJ_ERR_CUDA;
+    }
+}
+
+void check_schema(const phj_schema & s, const char * side)
+{
+    if (s.n_payloads > PHJ_MAX_PAYLOADS)
+        throw Error(PHJ_ERR_INVALID_ARGUMENT, std::string(side) + ": more than 8 payload columns");
+    for (uint32_t c = 0; c < s.n_payloads; ++c)
+        if (s.types[c] > PHJ_U128)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, std::string(side) + ": unknown payload type");
+}
+
+std::vector<uint32_t> check_bits(const uint8_t * bits, uint32_t n)
+{
+    if (n == 0 || bits == nullptr)
+        throw Error(PHJ_ERR_INVALID_ARGUMENT, "radixShuffle: at least one pass required");
+    std::vector<uint32_t> v;
+    uint32_t total = 0;
+    for (uint32_t i = 0; i < n; ++i)
+    {
+        if (bits[i] == 0 || bits[i] > 16)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "partition bits per pass must be in [1, 16]");
+        v.push_back(bits[i]);
+        total += bits[i];
+    }
+    if (total == 0 || total > 32)
+        throw Error(PHJ_ERR_INVALID_ARGUMENT, "radixShuffle: total partition bits must be in [1, 32]");
+    if (total > 24)
+        throw Error(PHJ_ERR_UNSUPPORTED, "device schemes support at most 24 total partition bits (16M leaves)");
+    return v;
+}
+
+void check_sides(const phj_table * b, const phj_table * p)
+{
+    if (!b || !p)
+        throw Error(PHJ_ERR_INVALID_ARGUMENT, "null build or probe table");
+    if (b->rows >= (1ull << 31) || p->rows >= (1ull << 32))
+        throw Error(PHJ_ERR_UNSUPPORTED, "device schemes support < 2^31 build rows and < 2^32 probe rows");
+}
+
+phj_output * new_output(phj_ctx * ctx, const phj_schema & left, const phj_schema & right, uint64_t cap)
+{
+    phj_output * o = new phj_output();
+    o->left = left;
+    o->right = right;
+    o->cap = cap;
+    try
+    {
+        o->keys = dalloc_n<uint64_t>(ctx, cap);
+        o->bytes += cap * 8;
+        for (uint32_t c = 0; c < left.n_payloads; ++c)
+        {
+            o->lcol[c] = dalloc(ctx, std::max<uint64_t>(1, cap * payload_width(left.types[c])));
+            o->bytes += cap * payload_width(left.types[c]);
+        }
+        for (uint32_t c = 0; c < right.n_payloads; ++c)
+        {
+            o->rcol[c] = dalloc(ctx, std::max<uint64_t>(1, cap * payload_width(right.types[c])));
+            o->bytes += cap * payload_width(right.types[c]);
+        }
+    }
+    catch (...)
+    {
+        dfree(ctx, o->keys);
+        for (uint32_t c = 0; c < PHJ_MAX_PAYLOADS; ++c)
+        {
+            dfree(ctx, o->lcol[c]);
+            dfree(ctx, o->rcol[c]);
+        }
+        delete o;
+        throw;
+    }
+    return o;
+}
+
+void free_output(phj_ctx * ctx, phj_output * o)
+{
+    if (!o)
+        return;
+    dfree(ctx, o->keys);
+    for (uint32_t c = 0; c < PHJ_MAX_PAYLOADS; ++c)
+    {
+        dfree(ctx, o->lcol[c]);
+        dfree(ctx, o->rcol[c]);
+    }
+    delete o;
+}
+
+void set_block_structure(phj_ctx * ctx, phj_table * t, uint32_t n_blocks, const uint32_t * block_rows)
+{
+    std::vector<uint64_t> off;
+    if (!block_rows || n_blocks == 0)
+    {
+        off = {0, t->rows};
+        t->n_blocks = 1;
+        t->uniform_block_rows = 0;
+    }
+    else
+    {
+        off.resize(n_blocks + 1);
+        off[0] = 0;
+        for (uint32_t b = 0; b < n_blocks; ++b)
+            off[b + 1] = off[b] + block_rows[b];
+        if (off[n_blocks] != t->rows)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "block_rows do not add up to total_rows");
+        t->n_blocks = n_blocks;
+        uint32_t u = block_rows[0];
+        for (uint32_t b = 0; b + 1 < n_blocks; ++b)
+            if (block_rows[b] != u)
+                u = 0;
+        if (u && block_rows[n_blocks - 1] > u)
+            u = 0;
+        t->uniform_block_rows = u;
+    }
+    t->block_off = dalloc_n<uint64_t>(ctx, off.size());
+    PHJ_CUDA(cudaMemcpyAsync(t->block_off, off.data(), off.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void free_table(phj_ctx * ctx, phj_table * t)
+{
+    if (!t)
+        return;
+    if (t->owned)
+    {
+        dfree(ctx, t->keys);
+        for (uint32_t c = 0; c < PHJ_MAX_PAYLOADS; ++c)
+            dfree(ctx, t->cols[c]);
+    }
+    dfree(ctx, t->block_off);
+    delete t;
+}
+
+phj_table * alloc_table(phj_ctx * ctx, const phj_schema & schema, uint64_t rows)
+{
+    phj_table * t = new phj_table();
+    t->schema = schema;
+    t->rows = rows;
+    t->owned = true;
+    try
+    {
+        t->keys = dalloc_n<uint64_t>(ctx, rows);
+        for (uint32_t c = 0; c < schema.n_payloads; ++c)
+            t->cols[c] = dalloc(ctx, std::max<uint64_t>(1, rows * payload_width(schema.types[c])));
+    }
+    catch (...)
+    {
+        free_table(ctx, t);
+        throw;
+    }
+    return t;
+}
+
+void fill_phase(phj_phase_timing & p, float ms, uint64_t rows)
+{
+    p.wall_ms = ms;
+    p.ns_per_row = rows ? (double)ms * 1e6 / (double)rows : 0.0;
+}
+
+// Whether the probe side's first radix pass is written out before probing.
+// Materialising orders the probe rows by leaf group so that the tables a
+// window of probe rows touches stay in L2; when every table plus the build
+// payloads fit in a fraction of L2 anyway, the pass only costs bandwidth.
+bool materialize_probe(phj_ctx * ctx, const LeafTables & lt, const phj_table & build, uint32_t n_leaves)
+{
+    if (ctx->probe_materialize >= 0)
+        return ctx->probe_materialize != 0;
+    const uint64_t table_bytes = lt.total_cells * sizeof(Cell) + (uint64_t)n_leaves * sizeof(LeafMeta);
+    const uint64_t build_bytes = build.rows * (8 + schema_bytes(build.schema)) + (lt.any_dup ? build.rows * 8 : 0);
+    return table_bytes + build_bytes > ctx->l2_bytes / 2;
+}
+
+Cols payload_cols(const Cols & c)
+{
+    Cols p = c;
+    p.keys = nullptr;
+    return p;
+}
+
+// Sizes the output: probe rows bound the output when no build key repeats;
+// otherwise a count-only probe gives the exact size first.
+phj_output * probe_into_output(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+{
+    uint64_t cap = a.probe_rows;
+    if (a.any_dup)
+        cap = probe_join(ctx, s, a, nullptr, true, "probe_count");
+    phj_output * out = new_output(ctx, left, right, cap);
+    try
+    {
+        out->rows = probe_join(ctx, s, a, out, false, "probe_join");
+        if (out->rows > out->cap)
+            throw Error(PHJ_ERR_CAPACITY, "probe produced more rows than its counted capacity");
+    }
+    catch (...)
+    {
+        free_output(ctx, out);
+        throw;
+    }
+    return out;
+}
+} // namespace
+
+// ---------------------------------------------------------------------------
+// schemes
+// ---------------------------------------------------------------------------
+static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj_output ** out, phj_chj_result * res)
+{
+    begin_run(ctx);
+    Scratch s(ctx);
+    cudaEvent_t e0 = take_event(ctx), e1 = take_event(ctx), e2 = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(e0, ctx->stream));
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(B.rows);
+    build_global_table(ctx, s, B, 8, lt);
+    PHJ_CUDA(cudaEventRecord(e1, ctx->stream));
+    ProbeArgs a{};
+    a.probe = cols_of(P);
+    a.probe_rows = P.rows;
+    a.build = payload_cols(cols_of(B));
+    a.meta = lt.meta;
+    a.cells = lt.cells;
+    a.next = lt.next;
+    a.leaf_bits = 8;
+    a.chj = 1;
+    a.block_off = B.block_off;
+    a.uniform_block_rows = B.uniform_block_rows;
+    a.any_dup = lt.any_dup;
+    phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
+    PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
+    PHJ_CUDA(cudaEventSynchronize(e2));
+    if (res)
+    {
+        fill_phase(res->build, event_ms(e0, e1), B.rows);
+        fill_phase(res->probe, event_ms(e1, e2), P.rows);
+        res->e2e_wall_ms = event_ms(e0, e2);
+        res->peak_mem_bytes = ctx->peak_bytes;
+    }
+    *out = o;
+}
+
+static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P, const std::vector<uint32_t> & bits, phj_output ** out,
+                         phj_phj_result * res)
+{
+    begin_run(ctx);
+    Scratch s(ctx);
+    uint32_t total_bits = 0;
+    for (uint32_t b : bits)
+        total_bits += b;
+    const uint32_t n_leaves = 1u << total_bits;
+    cudaEvent_t ev[5];
+    for (auto & e : ev)
+        e = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+
+    // -------- BUILD SHUFFLE (src/PHJ.cpp:220-223) --------
+    const Cols bin = cols_of(B);
+    const Cols bpart = alloc_cols_like(s, B.schema, B.rows);
+    const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
+    uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
+    radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+
+    // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(B.rows);
+    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
+    PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
+
+    // -------- PROBE SHUFFLE (src/PHJ.cpp:225-228): first pass only --------
+    ProbeArgs a{};
+    a.probe = cols_of(P);
+    if (materialize_probe(ctx, lt, B, n_leaves) && P.rows > 0)
+    {
+        const Cols ppart = alloc_cols_like(s, P.schema, P.rows);
+        const bool split = bits[0] > 11;
+        const Cols ptmp = split ? alloc_cols_like(s, P.schema, P.rows) : ppart;
+        uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
+        radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+        a.probe = ppart;
+    }
+    PHJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
+
+    // -------- PROBE with projection (src/PHJ.cpp:284-299) --------
+    a.probe_rows = P.rows;
+    a.build = payload_cols(bpart);
+    a.meta = lt.meta;
+    a.cells = lt.cells;
+    a.next = lt.next;
+    a.leaf_bits = total_bits;
+    a.chj = 0;
+    a.any_dup = lt.any_dup;
+    phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
+    PHJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
+    PHJ_CUDA(cudaEventSynchronize(ev[4]));
+    if (res)
+    {
+        fill_phase(res->build_shuffle, event_ms(ev[0], ev[1]), B.rows);
+        fill_phase(res->build, event_ms(ev[1], ev[2]), B.rows);
+        fill_phase(res->probe_shuffle, event_ms(ev[2], ev[3]), P.rows);
+        fill_phase(res->probe, event_ms(ev[3], ev[4]), P.rows);
+        res->e2e_wall_ms = event_ms(ev[0], ev[4]);
+        res->peak_mem_bytes = ctx->peak_bytes;
+    }
+    *out = o;
+}
+
+} // namespace phjg
+
+using namespace phjg;
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+uint32_t phj_abi_version(void)
+{
+    return PHJ_GPU_ABI_VERSION;
+}
+
+phj_status phj_ctx_create(int device, phj_ctx ** out)
+{
+    if (!out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0)
+    {
+        cudaGetLastError();
+        return PHJ_ERR_NO_DEVICE;
+    }
+    if (device < 0 || device >= n)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    phj_ctx * ctx = new (std::nothrow) phj_ctx();
+    if (!ctx)
+        return PHJ_ERR_OUT_OF_MEMORY;
+    const phj_status st = guard(ctx, [&] {
+        ctx->device = device;
+        PHJ_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop;
+        PHJ_CUDA(cudaGetDeviceProperties(&prop, device));
+        if (prop.major < 10)
+            throw Error(PHJ_ERR_UNSUPPORTED, "this library is built for sm_103a (Blackwell) only");
+        ctx->num_sms = prop.multiProcessorCount;
+        ctx->smem_optin = prop.sharedMemPerBlockOptin;
+        ctx->l2_bytes = prop.l2CacheSize;
+        PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        cudaMemPoolProps pp{};
+        pp.allocType = cudaMemAllocationTypePinned;
+        pp.location.type = cudaMemLocationTypeDevice;
+        pp.location.id = device;
+        PHJ_CUDA(cudaMemPoolCreate(&ctx->pool, &pp));
+        uint64_t keep = ~0ull; // keep freed memory in the pool across runs
+        PHJ_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        set_partition_smem_limits((int)ctx->smem_optin);
+        set_build_smem_limits((int)ctx->smem_optin);
+    });
+    if (st != PHJ_OK)
+    {
+        std::fprintf(stderr, "phj_ctx_create: %s\n", ctx->last_error.c_str());
+        phj_ctx_destroy(ctx);
+        return st;
+    }
+    *out = ctx;
+    return PHJ_OK;
+}
+
+void phj_ctx_destroy(phj_ctx * ctx)
+{
+    if (!ctx)
+        return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    if (ctx->l2_flush)
+        cudaFree(ctx->l2_flush);
+    for (cudaEvent_t e : ctx->event_pool)
+        cudaEventDestroy(e);
+    for (auto & lv : ctx->live)
+        cudaFreeAsync(lv.first, ctx->stream);
+    if (ctx->stream)
+        cudaStreamSynchronize(ctx->stream);
+    if (ctx->pool)
+        cudaMemPoolDestroy(ctx->pool);
+    if (ctx->stream)
+        cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+const char * phj_last_error(const phj_ctx * ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+void * phj_ctx_stream(phj_ctx * ctx)
+{
+    return ctx ? (void *)ctx->stream : nullptr;
+}
+
+phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
+{
+    if (!ctx || !name)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    if (std::strcmp(name, "probe_materialize") == 0 && value >= -1 && value <= 1)
+        ctx->probe_materialize = (int)value;
+    else if (std::strcmp(name, "time_kernels") == 0)
+        ctx->time_kernels = value != 0;
+    else
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return PHJ_OK;
+}
+
+phj_status phj_resolve_radix(uint64_t partitions, uint32_t passes, const uint8_t * bits_override, uint32_t n_bits_override, uint8_t * out_bits,
+                             uint32_t * out_n_passes)
+{
+    if (!out_bits || !out_n_passes)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    uint32_t total = 0;
+    if (n_bits_override > 0)
+    {
+        if (!bits_override || n_bits_override > 32)
+            return PHJ_ERR_INVALID_ARGUMENT;
+        for (uint32_t i = 0; i < n_bits_override; ++i)
+        {
+            if (bits_override[i] == 0 || bits_override[i] > 16) // CLI.cpp parseBitsList
+                return PHJ_ERR_INVALID_ARGUMENT;
+            out_bits[i] = bits_override[i];
+            total += bits_override[i];
+        }
+        *out_n_passes = n_bits_override;
+    }
+    else
+    {
+        const uint64_t parts = partitions == 0 ? 256 : partitions;
+        if ((parts & (parts - 1)) != 0)
+            return PHJ_ERR_INVALID_ARGUMENT; // --partitions must be a positive power of 2
+        uint32_t tb = 0;
+        while ((1ull << tb) < parts)
+            ++tb;
+        const uint32_t np = passes == 0 ? 1 : passes;
+        if (np > tb)
+            return PHJ_ERR_INVALID_ARGUMENT; // passes cannot exceed log2(partitions)
+        for (uint32_t p = 0; p < np; ++p)
+            out_bits[p] = (uint8_t)(tb / np + (p < tb % np ? 1u : 0u));
+        *out_n_passes = np;
+        total = tb;
+    }
+    if (total == 0 || total > 32)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return PHJ_OK;
+}
+
+static phj_status make_table(phj_ctx * ctx, const phj_block_stream * src, phj_table ** out, bool upload)
+{
+    if (!ctx || !src || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        check_schema(src->schema, "stream");
+        if (src->total_rows && !src->keys)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "null key column");
+        for (uint32_t c = 0; c < src->schema.n_payloads; ++c)
+            if (src->total_rows && !src->payloads[c])
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "null payload column");
+        phj_table * t = nullptr;
+        if (upload)
+        {
+            t = alloc_table(ctx, src->schema, src->total_rows);
+            const cudaMemcpyKind kind = src->location == PHJ_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+            try
+            {
+                if (src->total_rows)
+                {
+                    PHJ_CUDA(cudaMemcpyAsync(t->keys, src->keys, src->total_rows * 8, kind, ctx->stream));
+                    for (uint32_t c = 0; c < src->schema.n_payloads; ++c)
+                        PHJ_CUDA(cudaMemcpyAsync(t->cols[c], src->payloads[c], src->total_rows * payload_width(src->schema.types[c]), kind,
+                                                 ctx->stream));
+                }
+                set_block_structure(ctx, t, src->n_blocks, src->block_rows);
+            }
+            catch (...)
+            {
+                free_table(ctx, t);
+                throw;
+            }
+        }
+        else
+        {
+            if (src->location != PHJ_DEVICE)
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "phj_table_wrap_device needs device columns");
+            t = new phj_table();
+            t->schema = src->schema;
+            t->rows = src->total_rows;
+            t->keys = const_cast<uint64_t *>(src->keys);
+            for (uint32_t c = 0; c < src->schema.n_payloads; ++c)
+                t->cols[c] = const_cast<void *>(src->payloads[c]);
+            t->owned = false;
+            try
+            {
+                set_block_structure(ctx, t, src->n_blocks, src->block_rows);
+            }
+            catch (...)
+            {
+                free_table(ctx, t);
+                throw;
+            }
+        }
+        *out = t;
+    });
+}
+
+phj_status phj_table_upload(phj_ctx * ctx, const phj_block_stream * host_stream, phj_table ** out)
+{
+    return make_table(ctx, host_stream, out, true);
+}
+
+phj_status phj_table_wrap_device(phj_ctx * ctx, const phj_block_stream * device_stream, phj_table ** out)
+{
+    return make_table(ctx, device_stream, out, false);
+}
+
+phj_status phj_table_generate(phj_ctx * ctx, const phj_gen_spec * spec, phj_table ** out)
+{
+    if (!ctx || !spec || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        check_schema(spec->schema, "generated stream");
+        if (spec->kind > 5)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "unknown generator kind");
+        if (spec->rows >= (1ull << 32))
+            throw Error(PHJ_ERR_UNSUPPORTED, "generated streams hold < 2^32 rows");
+        if ((spec->kind == 3 || spec->kind == 4 || spec->kind == 5) && (spec->domain == 0 || spec->domain > (1ull << 32)))
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "generator domain must be in [1, 2^32]");
+        phj_table * t = alloc_table(ctx, spec->schema, spec->rows);
+        try
+        {
+            if (spec->rows)
+                t->gen_distinct = generate_rows(ctx, *spec, *t);
+            std::vector<uint32_t> br;
+            const uint32_t bs = spec->block_rows ? spec->block_rows : 10000;
+            for (uint64_t r = 0; r < spec->rows; r += bs)
+                br.push_back((uint32_t)std::min<uint64_t>(bs, spec->rows - r));
+            set_block_structure(ctx, t, (uint32_t)br.size(), br.empty() ? nullptr : br.data());
+        }
+        catch (...)
+        {
+            free_table(ctx, t);
+            throw;
+        }
+        *out = t;
+    });
+}
+
+phj_status phj_table_download(phj_ctx * ctx, const phj_table * t, uint64_t * keys, void * const * payloads)
+{
+    if (!ctx || !t)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] {
+        if (t->rows == 0)
+            return;
+        if (keys)
+            PHJ_CUDA(cudaMemcpyAsync(keys, t->keys, t->rows * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (payloads)
+            for (uint32_t c = 0; c < t->schema.n_payloads; ++c)
+                if (payloads[c])
+                    PHJ_CUDA(cudaMemcpyAsync(payloads[c], t->cols[c], t->rows * payload_width(t->schema.types[c]), cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+uint64_t phj_table_rows(const phj_table * t)
+{
+    return t ? t->rows : 0;
+}
+
+uint64_t phj_table_gen_distinct(const phj_table * t)
+{
+    return t ? t->gen_distinct : 0;
+}
+
+void phj_table_free(phj_ctx * ctx, phj_table * t)
+{
+    if (ctx)
+        free_table(ctx, t);
+}
+
+phj_status phj_run_chj(phj_ctx * ctx, const phj_table * build, const phj_table * probe, phj_output ** out, phj_chj_result * result)
+{
+    if (!ctx || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        check_sides(build, probe);
+        run_chj(ctx, *build, *probe, out, result);
+    });
+}
+
+phj_status phj_run_phj_pure(phj_ctx * ctx, const phj_table * build, const phj_table * probe, const uint8_t * pass_bits, uint32_t n_passes,
+                            phj_output ** out, phj_phj_result * result)
+{
+    if (!ctx || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        const std::vector<uint32_t> bits = check_bits(pass_bits, n_passes);
+        check_sides(build, probe);
+        run_phj_pure(ctx, *build, *probe, bits, out, result);
+    });
+}
+
+phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_table * probe, const uint8_t * pass_bits, uint32_t n_passes,
+                           uint64_t bep_budget_mib, uint32_t workers, phj_output ** out, phj_bep_result * result)
+{
+    if (!ctx || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    (void)bep_budget_mib;
+    (void)workers;
+    (void)result;
+    return guard(ctx, [&] {
+        (void)check_bits(pass_bits, n_passes);
+        check_sides(build, probe);
+        throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) device scheme not built yet");
+    });
+}
+
+uint64_t phj_output_rows(const phj_output * out)
+{
+    return out ? out->rows : 0;
+}
+
+phj_status phj_output_device_columns(const phj_output * out, const uint64_t ** keys, const void ** left, const void ** right)
+{
+    if (!out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    if (keys)
+        *keys = out->keys;
+    if (left)
+        for (uint32_t c = 0; c < out->left.n_payloads; ++c)
+            left[c] = out->lcol[c];
+    if (right)
+        for (uint32_t c = 0; c < out->right.n_payloads; ++c)
+            right[c] = out->rcol[c];
+    return PHJ_OK;
+}
+
+phj_status phj_output_download(phj_ctx * ctx, const phj_output * out, uint64_t * keys, void * const * left, void * const * right)
+{
+    if (!ctx || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] {
+        const uint64_t n = out->rows;
+        if (n == 0)
+            return;
+        if (keys)
+            PHJ_CUDA(cudaMemcpyAsync(keys, out->keys, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+        if (left)
+            for (uint32_t c = 0; c < out->left.n_payloads; ++c)
+                if (left[c])
+                    PHJ_CUDA(cudaMemcpyAsync(left[c], out->lcol[c], n * payload_width(out->left.types[c]), cudaMemcpyDeviceToHost, ctx->stream));
+        if (right)
+            for (uint32_t c = 0; c < out->right.n_payloads; ++c)
+                if (right[c])
+                    PHJ_CUDA(
+                        cudaMemcpyAsync(right[c], out->rcol[c], n * payload_width(out->right.types[c]), cudaMemcpyDeviceToHost, ctx->stream));
+        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    });
+}
+
+phj_status phj_output_fingerprint(phj_ctx * ctx, const phj_output * out, uint64_t fp[3])
+{
+    if (!ctx || !out || !fp)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] { fingerprint(ctx, *out, fp); });
+}
+
+void phj_output_free(phj_ctx * ctx, phj_output * out)
+{
+    if (ctx)
+        free_output(ctx, out);
+}
+
+uint32_t phj_last_kernel_times(const phj_ctx * ctx, phj_kernel_time * out, uint32_t cap)
+{
+    if (!ctx || !out)
+        return 0;
+    uint32_t n = 0;
+    for (const auto & r : ctx->records)
+    {
+        if (n >= cap)
+            break;
+        phj_kernel_time & k = out[n++];
+        std::memset(&k, 0, sizeof(k));
+        std::strncpy(k.name, r.name.c_str(), sizeof(k.name) - 1);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, r.start, r.stop) != cudaSuccess)
+        {
+            cudaGetLastError();
+            ms = -1.f;
+        }
+        k.ms = ms;
+        k.rows = r.rows;
+        k.bytes = r.bytes;
+    }
+    return n;
+}
+
+uint64_t phj_launch_count(const phj_ctx * ctx)
+{
+    return ctx ? ctx->launches : 0;
+}
+
+phj_status phj_host_alloc(phj_ctx * ctx, size_t bytes, void ** out)
+{
+    if (!ctx || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] { PHJ_CUDA(cudaHostAlloc(out, bytes ? bytes : 1, cudaHostAllocDefault)); });
+}
+
+void phj_host_free(phj_ctx * ctx, void * p)
+{
+    (void)ctx;
+    if (p)
+        cudaFreeHost(p);
+}
+
+phj_status phj_flush_l2(phj_ctx * ctx)
+{
+    if (!ctx)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return guard(ctx, [&] {
+        if (!ctx->l2_flush)
+        {
+            ctx->l2_flush_bytes = std::max<size_t>(ctx->l2_bytes * 2, 256u << 20);
+            PHJ_CUDA(cudaMalloc(&ctx->l2_flush, ctx->l2_flush_bytes));
+        }
+        PHJ_CUDA(cudaMemsetAsync(ctx->l2_flush, ctx->launches & 0xff, ctx->l2_flush_bytes, ctx->stream));
+    });
+}
+
+} // extern "C"

@@ -1,0 +1,248 @@
+// build.cu -- hashtable build on the device.
+//
+// PHJ-PURE / PHJ: one JoinHashTable per leaf (src/PHJ.cpp:260-282,
+// src/PHJBep.cpp:192-232).  Capacity follows JoinHashTable::reserve
+// (src/HashTable.h:72-79): bit_ceil(2 * rows), i.e. load <= 1/2.  One CTA
+// owns a leaf: it builds the table in shared memory with 128-bit CAS
+// inserts, threads each row's previous head into the next-chain
+// (BlockStore::setPrev, src/BlockStore.h:83-84; buildOneBlock,
+// src/JoinOps.h:205-228), then streams the finished table to global memory.
+// Leaves too large for shared memory are built in place in global memory.
+//
+// CHJ: one global table of 256 sub-tables selected by the top 8 hash bits
+// (the mutex-free form of ChjSlottedTable, src/TwoLevelHashTable.h:57-91),
+// filled by every thread of the grid with 128-bit CAS inserts.
+#include "internal.h"
+
+namespace phjg
+{
+namespace
+{
+constexpr int kBuildNT = 256;
+constexpr uint32_t kSmemCellsMax = 8192; // 128 KiB of cells per CTA
+
+__global__ void k_leaf_caps(const uint32_t * __restrict__ leaf_off, uint32_t n_leaves, uint32_t * __restrict__ caps, uint32_t * __restrict__ max_rows)
+{
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_leaves)
+        return;
+    const uint32_t r = leaf_off[l + 1] - leaf_off[l];
+    caps[l] = r ? (uint32_t)bit_ceil64(2ull * r) : 0u;
+    if (r)
+        atomicMax(max_rows, r);
+}
+
+__device__ __forceinline__ uint32_t log2u(uint64_t x)
+{
+    return 63u - (uint32_t)__clzll((long long)x);
+}
+
+__global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __restrict__ keys, const uint32_t * __restrict__ leaf_off,
+                                                         const uint32_t * __restrict__ table_off, uint32_t smem_cells, Cell * __restrict__ cells,
+                                                         uint64_t * __restrict__ next, LeafMeta * __restrict__ meta, int * __restrict__ any_dup)
+{
+    extern __shared__ __align__(16) Cell sh_cells[];
+    __shared__ int dup;
+    const uint32_t l = blockIdx.x;
+    const uint32_t r0 = leaf_off[l], r = leaf_off[l + 1] - r0;
+    const uint64_t t0 = table_off[l];
+    const uint64_t cap = table_off[l + 1] - t0;
+    if (threadIdx.x == 0)
+        dup = 0;
+    if (r == 0)
+    {
+        if (threadIdx.x == 0)
+            meta[l] = LeafMeta{t0, r0, 0, 0, 0, 0};
+        return;
+    }
+    const Cell empty{0ull, INVALID_REF};
+    const bool in_smem = cap <= smem_cells;
+    Cell * tab = in_smem ? sh_cells : cells + t0;
+    for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT)
+        tab[i] = empty;
+    __syncthreads();
+    bool my_dup = false;
+    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+    {
+        const uint64_t k = keys[r0 + i];
+        const uint64_t h = int_hash64(k);
+        const uint64_t ref = make_ref(l, i);
+        const uint64_t prev = in_smem ? table_insert<true>(tab, cap, h, k, ref) : table_insert<false>(tab, cap, h, k, ref);
+        next[r0 + i] = prev;
+        my_dup |= ref_valid(prev);
+    }
+    if (__any_sync(0xffffffffu, my_dup) && (threadIdx.x & 31) == 0)
+        dup = 1;
+    __syncthreads();
+    if (in_smem)
+    {
+        ulonglong2 * dst = reinterpret_cast<ulonglong2 *>(cells + t0);
+        const ulonglong2 * src = reinterpret_cast<const ulonglong2 *>(sh_cells);
+        for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT)
+            dst[i] = src[i];
+    }
+    if (threadIdx.x == 0)
+    {
+        meta[l] = LeafMeta{t0, r0, (uint8_t)log2u(cap), 1, (uint8_t)dup, 0};
+        if (dup)
+            atomicOr(any_dup, 1);
+    }
+}
+
+// ---- CHJ --------------------------------------------------------------------
+
+__global__ void k_slot_hist(const uint64_t * __restrict__ keys, uint64_t n, uint32_t slot_bits, uint32_t * __restrict__ counts)
+{
+    extern __shared__ uint32_t bins[];
+    const uint32_t nb = 1u << slot_bits;
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+        bins[i] = 0;
+    __syncthreads();
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&bins[int_hash64(keys[i]) >> (64 - slot_bits)], 1u);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < nb; i += blockDim.x)
+        if (bins[i])
+            atomicAdd(&counts[i], bins[i]);
+}
+
+__global__ void k_slot_meta(const uint32_t * __restrict__ counts, const uint32_t * __restrict__ table_off, uint32_t n_slots, LeafMeta * __restrict__ meta)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= n_slots)
+        return;
+    const uint64_t cap = table_off[s + 1] - table_off[s];
+    meta[s] = LeafMeta{table_off[s], 0u, cap ? (uint8_t)log2u(cap) : (uint8_t)0, (uint8_t)(counts[s] != 0), 0, 0};
+}
+
+__global__ void k_fill_empty(Cell * __restrict__ cells, uint64_t n)
+{
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        reinterpret_cast<ulonglong2 *>(cells)[i] = make_ulonglong2(0ull, INVALID_REF);
+}
+
+__device__ __forceinline__ uint32_t block_of_row(uint64_t g, const uint64_t * __restrict__ block_off, uint32_t n_blocks, uint32_t uniform)
+{
+    if (uniform)
+        return (uint32_t)(g / uniform);
+    uint32_t lo = 0, hi = n_blocks; // block_off[lo] <= g < block_off[hi]
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (block_off[mid] <= g)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_chj_insert(const uint64_t * __restrict__ keys, uint64_t n, uint32_t slot_bits, const uint64_t * __restrict__ block_off,
+                             uint32_t n_blocks, uint32_t uniform, Cell * __restrict__ cells, LeafMeta * __restrict__ meta, uint64_t * __restrict__ next,
+                             int * __restrict__ any_dup)
+{
+    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < n; g += (uint64_t)gridDim.x * blockDim.x)
+    {
+        const uint64_t k = keys[g];
+        const uint64_t h = int_hash64(k);
+        const uint32_t s = (uint32_t)(h >> (64 - slot_bits));
+        const uint32_t b = block_of_row(g, block_off, n_blocks, uniform);
+        const uint32_t row = (uint32_t)(g - block_off[b]);
+        const LeafMeta m = meta[s];
+        const uint64_t prev = table_insert<false>(cells + m.table_off, 1ull << m.log2cap, h, k, make_ref(b, row));
+        next[g] = prev;
+        if (ref_valid(prev))
+        {
+            meta[s].dup = 1; // idempotent byte store
+            *any_dup = 1;
+        }
+    }
+}
+} // namespace
+
+void set_build_smem_limits(int smem_optin)
+{
+    const size_t need = (size_t)kSmemCellsMax * sizeof(Cell);
+    PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
+}
+
+void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves, LeafTables & lt)
+{
+    uint32_t * caps = s.get<uint32_t>(n_leaves + 1);
+    uint32_t * table_off = s.get<uint32_t>(n_leaves + 1);
+    uint32_t * small = s.get<uint32_t>(4); // [0] max rows, [1] any dup
+    PHJ_CUDA(cudaMemsetAsync(small, 0, 4 * sizeof(uint32_t), ctx->stream));
+    k_leaf_caps<<<(unsigned)ceil_div(n_leaves, 256), 256, 0, ctx->stream>>>(leaf_off, n_leaves, caps, small);
+    PHJ_LAUNCHED(ctx, "leaf_caps");
+    scan_u32(ctx, s, caps, table_off, n_leaves);
+    uint32_t host[2] = {0, 0};
+    PHJ_CUDA(cudaMemcpyAsync(&host[0], small, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaMemcpyAsync(&host[1], table_off + n_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    lt.max_rows = host[0];
+    lt.total_cells = host[1];
+    lt.meta = s.get<LeafMeta>(n_leaves);
+    lt.cells = s.get<Cell>(lt.total_cells);
+    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
+    const uint32_t smem_cells = (uint32_t)std::min<uint64_t>(max_cap, kSmemCellsMax);
+    int * any_dup = reinterpret_cast<int *>(small + 1);
+    {
+        KTimer kt(ctx, "build_leaf_tables", 0, 0);
+        k_build_leaf<<<n_leaves, kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, smem_cells, lt.cells,
+                                                                                            lt.next, lt.meta, any_dup);
+        PHJ_LAUNCHED(ctx, "build_leaf");
+    }
+    PHJ_CUDA(cudaMemcpyAsync(&lt.any_dup, any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uint32_t slot_bits, LeafTables & lt)
+{
+    const uint32_t n_slots = 1u << slot_bits;
+    uint32_t * counts = s.get<uint32_t>(n_slots + 1);
+    uint32_t * caps = s.get<uint32_t>(n_slots + 1);
+    uint32_t * table_off = s.get<uint32_t>(n_slots + 1);
+    int * any_dup = s.get<int>(1);
+    PHJ_CUDA(cudaMemsetAsync(counts, 0, (n_slots + 1) * sizeof(uint32_t), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(any_dup, 0, sizeof(int), ctx->stream));
+    const uint64_t n = build.rows;
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(n, 256), (uint64_t)ctx->num_sms * 8));
+    {
+        KTimer kt(ctx, "chj_slot_hist", n, n * 8);
+        k_slot_hist<<<grid, 256, n_slots * sizeof(uint32_t), ctx->stream>>>(build.keys, n, slot_bits, counts);
+        PHJ_LAUNCHED(ctx, "chj_slot_hist");
+    }
+    uint32_t * max_rows = s.get<uint32_t>(1);
+    PHJ_CUDA(cudaMemsetAsync(max_rows, 0, sizeof(uint32_t), ctx->stream));
+    // counts -> capacities -> offsets: the offsets of leaf_off-style caps
+    // reuse k_leaf_caps on a prefix of the counts.
+    uint32_t * cnt_off = s.get<uint32_t>(n_slots + 1);
+    scan_u32(ctx, s, counts, cnt_off, n_slots);
+    k_leaf_caps<<<(unsigned)ceil_div(n_slots, 256), 256, 0, ctx->stream>>>(cnt_off, n_slots, caps, max_rows);
+    PHJ_LAUNCHED(ctx, "chj_caps");
+    scan_u32(ctx, s, caps, table_off, n_slots);
+    uint32_t total = 0;
+    PHJ_CUDA(cudaMemcpyAsync(&total, table_off + n_slots, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    lt.total_cells = total;
+    lt.meta = s.get<LeafMeta>(n_slots);
+    lt.cells = s.get<Cell>(total);
+    k_slot_meta<<<(unsigned)ceil_div(n_slots, 256), 256, 0, ctx->stream>>>(counts, table_off, n_slots, lt.meta);
+    PHJ_LAUNCHED(ctx, "chj_meta");
+    {
+        KTimer kt(ctx, "chj_fill", 0, total * 16ull);
+        k_fill_empty<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(total, 256), (uint64_t)ctx->num_sms * 16)), 256, 0, ctx->stream>>>(
+            lt.cells, total);
+        PHJ_LAUNCHED(ctx, "chj_fill");
+    }
+    {
+        KTimer kt(ctx, "chj_insert", n, n * 16);
+        k_chj_insert<<<grid, 256, 0, ctx->stream>>>(build.keys, n, slot_bits, build.block_off, build.n_blocks, build.uniform_block_rows, lt.cells,
+                                                   lt.meta, lt.next, any_dup);
+        PHJ_LAUNCHED(ctx, "chj_insert");
+    }
+    PHJ_CUDA(cudaMemcpyAsync(&lt.any_dup, any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+} // namespace phjg

@@ -1,0 +1,207 @@
+// common.cuh -- device primitives shared by every kernel of the GB300 join
+// path: the join hash, the 16-byte (key, RowRefCell) cell with 128-bit CAS,
+// column descriptors, and small block-wide helpers.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace phjg
+{
+
+// ---------------------------------------------------------------------------
+// intHash64 (src/Hash.h:18-25): salt xor, then the Murmur3 fmix64 finaliser.
+// The constants define the function, so they are necessarily the same.
+// ---------------------------------------------------------------------------
+__host__ __device__ __forceinline__ uint64_t int_hash64(uint64_t x)
+{
+    x ^= 0x4cf5ad432745937fULL;
+    x = (x ^ (x >> 33)) * 0xff51afd7ed558ccdULL;
+    x = (x ^ (x >> 33)) * 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+// RowRefCell (src/Types.h:95-104) packed in one u64: block_no in the low
+// word, row_no in the high word, i.e. the little-endian image of the struct.
+constexpr uint32_t INVALID_BLOCK = 0xFFFFFFFFu;
+constexpr uint64_t INVALID_REF = 0x00000000FFFFFFFFull; // {INVALID_BLOCK, 0}
+
+__host__ __device__ __forceinline__ uint64_t make_ref(uint32_t block_no, uint32_t row_no)
+{
+    return (uint64_t)block_no | ((uint64_t)row_no << 32);
+}
+__host__ __device__ __forceinline__ uint32_t ref_block(uint64_t r) { return (uint32_t)r; }
+__host__ __device__ __forceinline__ uint32_t ref_row(uint64_t r) { return (uint32_t)(r >> 32); }
+__host__ __device__ __forceinline__ bool ref_valid(uint64_t r) { return (uint32_t)r != INVALID_BLOCK; }
+
+// JoinHashTable::Cell (src/HashTable.h:33-38): {u64 key; RowRefCell ref}.
+// Empty cell = {0, INVALID_REF} (src/HashTable.h:150), so key 0 stays legal.
+struct __align__(16) Cell
+{
+    uint64_t key;
+    uint64_t ref;
+};
+
+// 128-bit compare-and-swap on a cell (PTX atom.cas.b128, sm_90+).  Returns
+// the cell's previous contents as one atomic snapshot.
+__device__ __forceinline__ Cell cas_cell_global(Cell *p, Cell cmp, Cell val)
+{
+    Cell old;
+    asm volatile(
+        "{\n\t.reg .b128 c, v, o;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 v, {%4, %5};\n\t"
+        "atom.global.cas.b128 o, [%6], c, v;\n\t"
+        "mov.b128 {%0, %1}, o;\n\t}"
+        : "=l"(old.key), "=l"(old.ref)
+        : "l"(cmp.key), "l"(cmp.ref), "l"(val.key), "l"(val.ref), "l"(p)
+        : "memory");
+    return old;
+}
+
+__device__ __forceinline__ Cell cas_cell_shared(Cell *p, Cell cmp, Cell val)
+{
+    Cell old;
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    asm volatile(
+        "{\n\t.reg .b128 c, v, o;\n\t"
+        "mov.b128 c, {%2, %3};\n\t"
+        "mov.b128 v, {%4, %5};\n\t"
+        "atom.shared.cas.b128 o, [%6], c, v;\n\t"
+        "mov.b128 {%0, %1}, o;\n\t}"
+        : "=l"(old.key), "=l"(old.ref)
+        : "l"(cmp.key), "l"(cmp.ref), "l"(val.key), "l"(val.ref), "r"(a)
+        : "memory");
+    return old;
+}
+
+// Insert (key, ref) into an open-addressing table of `cap` (power of two)
+// cells with linear probing from `hash & (cap-1)` (src/HashTable.h:84-109).
+// Returns the previous head ref for `key` (INVALID_REF when new), which the
+// caller threads into the next-chain.  Concurrent inserters are safe: an
+// empty cell is claimed with one 128-bit CAS; a cell that already holds the
+// key gets its ref half swapped with a 64-bit exchange.  A claimed cell's
+// key never changes, so the CAS snapshot decides every step.  The loop is
+// bounded by `cap` steps (a table is never full: load <= 1/2).
+template <bool kShared>
+__device__ __forceinline__ uint64_t table_insert(Cell *cells, uint64_t cap, uint64_t hash, uint64_t key, uint64_t ref)
+{
+    const uint64_t mask = cap - 1;
+    uint64_t pos = hash & mask;
+    const Cell empty{0ull, INVALID_REF};
+    const Cell mine{key, ref};
+    for (uint64_t step = 0; step < cap; ++step)
+    {
+        Cell *c = cells + pos;
+        const Cell old = kShared ? cas_cell_shared(c, empty, mine) : cas_cell_global(c, empty, mine);
+        if (old.key == 0ull && old.ref == INVALID_REF)
+            return INVALID_REF;
+        if (old.key == key)
+            return (uint64_t)atomicExch((unsigned long long *)&c->ref, (unsigned long long)ref);
+        pos = (pos + 1) & mask;
+    }
+    return INVALID_REF; // unreachable for tables at <= 50% load
+}
+
+// Lookup after the build barrier (src/HashTable.h:112-127): plain loads.
+__device__ __forceinline__ uint64_t table_find(const Cell *cells, uint64_t cap, uint64_t hash, uint64_t key)
+{
+    if (cap == 0)
+        return INVALID_REF;
+    const uint64_t mask = cap - 1;
+    uint64_t pos = hash & mask;
+    for (uint64_t step = 0; step < cap; ++step)
+    {
+        const ulonglong2 c = __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
+        if (!ref_valid(c.y))
+            return INVALID_REF;
+        if (c.x == key)
+            return c.y;
+        pos = (pos + 1) & mask;
+    }
+    return INVALID_REF;
+}
+
+// ---------------------------------------------------------------------------
+// Column descriptors.  A side (build or probe) is a key column plus up to
+// kMaxCols payload columns of width 1/2/4/8/16 bytes, all column-major.
+// ---------------------------------------------------------------------------
+constexpr int kMaxCols = 8;
+
+struct Cols
+{
+    uint64_t *keys;
+    void *col[kMaxCols];
+    uint8_t width[kMaxCols];
+    uint32_t n;
+};
+
+// Copy element `src_i` of a column to element `dst_i` of another column of
+// the same width.
+__device__ __forceinline__ void copy_elem(void *dst, uint64_t dst_i, const void *src, uint64_t src_i, uint32_t w)
+{
+    switch (w)
+    {
+        case 1: static_cast<uint8_t *>(dst)[dst_i] = static_cast<const uint8_t *>(src)[src_i]; break;
+        case 2: static_cast<uint16_t *>(dst)[dst_i] = static_cast<const uint16_t *>(src)[src_i]; break;
+        case 4: static_cast<uint32_t *>(dst)[dst_i] = static_cast<const uint32_t *>(src)[src_i]; break;
+        case 8: static_cast<uint64_t *>(dst)[dst_i] = static_cast<const uint64_t *>(src)[src_i]; break;
+        default: static_cast<uint4 *>(dst)[dst_i] = static_cast<const uint4 *>(src)[src_i]; break;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Block-wide exclusive scan of one u32 per thread (NT threads, NT % 32 == 0).
+// `warp_sums` must hold NT/32 entries of shared memory.  Returns the
+// exclusive prefix; *total gets the block sum.
+// ---------------------------------------------------------------------------
+template <int NT>
+__device__ __forceinline__ uint32_t block_excl_scan(uint32_t v, uint32_t *warp_sums, uint32_t *total)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o)
+            x += y;
+    }
+    if (lane == 31)
+        warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0)
+    {
+        uint32_t s = lane < NT / 32 ? warp_sums[lane] : 0u;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1)
+        {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o)
+                s += y;
+        }
+        if (lane < NT / 32)
+            warp_sums[lane] = s; // inclusive warp prefix
+    }
+    __syncthreads();
+    const uint32_t warp_base = warp == 0 ? 0u : warp_sums[warp - 1];
+    *total = warp_sums[NT / 32 - 1];
+    const uint32_t excl = warp_base + x - v;
+    __syncthreads(); // warp_sums may be reused by the caller
+    return excl;
+}
+
+__host__ __device__ __forceinline__ uint64_t ceil_div(uint64_t a, uint64_t b) { return (a + b - 1) / b; }
+
+__host__ __device__ __forceinline__ uint64_t bit_ceil64(uint64_t x)
+{
+    if (x <= 1)
+        return 1;
+    uint64_t p = 1;
+    while (p < x)
+        p <<= 1;
+    return p;
+}
+
+} // namespace phjg

@@ -1,0 +1,237 @@
+// internal.h -- host-side internals shared by the library's translation
+// units: the context, device tables and outputs, the stream-ordered
+// allocator, kernel timing, and the entry points of each kernel module.
+#pragma once
+
+#include <algorithm>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/phj_gpu.h"
+#include "common.cuh"
+
+// ---------------------------------------------------------------------------
+// Errors inside the library are C++ exceptions; the C ABI turns them into a
+// status code plus phj_last_error().
+// ---------------------------------------------------------------------------
+namespace phjg
+{
+struct Error : std::runtime_error
+{
+    phj_status status;
+    Error(phj_status s, const std::string & m)
+        : std::runtime_error(m)
+        , status(s)
+    {
+    }
+};
+
+void cuda_check(cudaError_t e, const char * what, const char * file, int line);
+#define PHJ_CUDA(call) ::phjg::cuda_check((call), #call, __FILE__, __LINE__)
+#define PHJ_LAUNCHED(ctx, name) ::phjg::after_launch((ctx), (name), __FILE__, __LINE__)
+
+struct KernelRecord
+{
+    std::string name;
+    cudaEvent_t start = nullptr, stop = nullptr;
+    uint64_t rows = 0, bytes = 0;
+};
+
+inline uint32_t payload_width(uint8_t t)
+{
+    switch (t)
+    {
+        case PHJ_U8: return 1;
+        case PHJ_U16: return 2;
+        case PHJ_U32: return 4;
+        case PHJ_U64: return 8;
+        case PHJ_U128: return 16;
+        default: return 0;
+    }
+}
+
+inline uint64_t schema_bytes(const phj_schema & s)
+{
+    uint64_t b = 0;
+    for (uint32_t c = 0; c < s.n_payloads; ++c)
+        b += payload_width(s.types[c]);
+    return b;
+}
+} // namespace phjg
+
+struct phj_ctx
+{
+    int device = 0;
+    int num_sms = 0;
+    size_t smem_optin = 0;
+    size_t l2_bytes = 0;
+    cudaStream_t stream = nullptr;
+    cudaMemPool_t pool = nullptr;
+    std::string last_error;
+    uint64_t launches = 0;
+    // Allocation accounting of the current run (peak_mem_bytes).
+    uint64_t cur_bytes = 0, peak_bytes = 0;
+    std::vector<std::pair<void *, uint64_t>> live; // small: a run holds tens of buffers
+    // Per-kernel timing of the last run.
+    bool time_kernels = true;
+    std::vector<phjg::KernelRecord> records;
+    std::vector<cudaEvent_t> event_pool;
+    size_t event_next = 0;
+    void * l2_flush = nullptr;
+    size_t l2_flush_bytes = 0;
+    // Options (phj_ctx_set_int).
+    int probe_materialize = -1; // -1 auto, 0 never, 1 always
+};
+
+struct phj_table
+{
+    phj_schema schema{};
+    uint64_t rows = 0;
+    uint32_t n_blocks = 0;
+    uint64_t * keys = nullptr;
+    void * cols[PHJ_MAX_PAYLOADS] = {};
+    uint64_t * block_off = nullptr; // device, n_blocks + 1 (row offset of each block)
+    uint32_t uniform_block_rows = 0; // all blocks but the last have this many rows (0: irregular)
+    bool owned = false;
+    uint64_t gen_distinct = 0; // distinct build keys of a generated multi-match side
+};
+
+struct phj_output
+{
+    uint64_t rows = 0, cap = 0;
+    phj_schema left{}, right{};
+    uint64_t * keys = nullptr;
+    void * lcol[PHJ_MAX_PAYLOADS] = {};
+    void * rcol[PHJ_MAX_PAYLOADS] = {};
+    uint64_t bytes = 0;
+};
+
+namespace phjg
+{
+// ----- allocation (stream-ordered pool of the context) ---------------------
+void * dalloc(phj_ctx * ctx, size_t bytes);
+void dfree(phj_ctx * ctx, void * p);
+void reset_accounting(phj_ctx * ctx);
+
+template <class T>
+T * dalloc_n(phj_ctx * ctx, uint64_t n)
+{
+    return static_cast<T *>(dalloc(ctx, (size_t)(n ? n : 1) * sizeof(T)));
+}
+
+// RAII holder for run-scoped scratch.
+struct Scratch
+{
+    phj_ctx * ctx;
+    std::vector<void *> ptrs;
+    explicit Scratch(phj_ctx * c)
+        : ctx(c)
+    {
+    }
+    ~Scratch()
+    {
+        for (void * p : ptrs)
+            dfree(ctx, p);
+    }
+    template <class T>
+    T * get(uint64_t n)
+    {
+        T * p = dalloc_n<T>(ctx, n);
+        ptrs.push_back(p);
+        return p;
+    }
+    Scratch(const Scratch &) = delete;
+    Scratch & operator=(const Scratch &) = delete;
+};
+
+// ----- timing ----------------------------------------------------------------
+cudaEvent_t take_event(phj_ctx * ctx);
+void begin_run(phj_ctx * ctx);
+// Records an event pair around the next launch(es) when kernel timing is on.
+struct KTimer
+{
+    phj_ctx * ctx;
+    int idx = -1;
+    KTimer(phj_ctx * c, const char * name, uint64_t rows, uint64_t bytes);
+    ~KTimer();
+};
+void after_launch(phj_ctx * ctx, const char * name, const char * file, int line);
+float event_ms(cudaEvent_t a, cudaEvent_t b);
+
+// ----- columns ----------------------------------------------------------------
+Cols cols_of(const phj_table & t);
+Cols alloc_cols_like(Scratch & s, const phj_schema & schema, uint64_t rows);
+uint32_t max_width(const Cols & c);
+
+// ----- scan.cu -----------------------------------------------------------------
+// Exclusive scan of m u32 values into out[0..m); out[m] = total.
+void scan_u32(phj_ctx * ctx, Scratch & s, const uint32_t * in, uint32_t * out, uint64_t m);
+
+// ----- partition.cu ---------------------------------------------------------------
+// Radix-partitions n rows by the top sum(pass_bits) bits of intHash64(key)
+// (src/RadixPartition.cpp:546-577).  Rows land in `out` in leaf order;
+// leaf_off[0..2^bits] receives each leaf's first row (leaf_off[2^bits] = n).
+// Passes wider than kMaxPassBits are run as several physical passes.
+void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, const std::vector<uint32_t> & pass_bits,
+                     const Cols & out, const Cols & tmp, uint32_t * leaf_off, const char * phase);
+
+// ----- build.cu -----------------------------------------------------------------------
+// Leaf (or sub-table) directory entry: where a table lives and how big it is.
+struct __align__(16) LeafMeta
+{
+    uint64_t table_off; // first cell
+    uint32_t row_off;   // first build row of the leaf (PHJ) / unused (CHJ)
+    uint8_t log2cap;    // capacity = 1 << log2cap, 0 cells when has_table == 0
+    uint8_t has_table;
+    uint8_t dup;        // some key of this table has more than one build row
+    uint8_t pad;
+};
+
+struct LeafTables
+{
+    LeafMeta * meta = nullptr; // n_leaves
+    Cell * cells = nullptr;
+    uint64_t * next = nullptr; // next-chain, one RowRefCell per build row (BlockStore next_chain_)
+    uint64_t total_cells = 0;
+    uint32_t max_rows = 0;
+    int any_dup = 0;
+};
+
+// Per-leaf tables over leaf-partitioned build rows (PHJ-PURE / PHJ).
+void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves,
+                       LeafTables & lt);
+// One global table of 2^slot_bits sub-tables namespaced by the top hash bits (CHJ).
+void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uint32_t slot_bits, LeafTables & lt);
+
+// ----- probe.cu -------------------------------------------------------------------------
+struct ProbeArgs
+{
+    Cols probe;             // probe rows in the order they are streamed
+    uint64_t probe_rows;
+    Cols build;             // build payloads addressed by RowRefCell
+    const LeafMeta * meta;
+    const Cell * cells;
+    const uint64_t * next;
+    uint32_t leaf_bits;     // leaf = hash >> (64 - leaf_bits)
+    int chj;                // 1: refs are (input block, row); 0: refs are (leaf, row in leaf)
+    const uint64_t * block_off;
+    uint32_t uniform_block_rows;
+    int any_dup;
+};
+// Returns the number of output rows; writes them to `out` unless count_only.
+uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name);
+
+// ----- gen.cu -----------------------------------------------------------------------------
+// Fills t's columns; returns the number of distinct build keys for kinds 0/2.
+uint64_t generate_rows(phj_ctx * ctx, const phj_gen_spec & spec, phj_table & t);
+void fingerprint(phj_ctx * ctx, const phj_output & out, uint64_t fp[3]);
+
+// ----- per-module kernel attributes (dynamic shared memory opt-in) -------------
+void set_partition_smem_limits(int smem_optin);
+void set_build_smem_limits(int smem_optin);
+
+} // namespace phjg

@@ -1,0 +1,354 @@
+// partition.cu -- radix partitioning on the top bits of intHash64
+// (src/RadixPartition.cpp: scatterBatch :316-393, radixShuffle :546-577,
+// refineToLeaves :417-539).
+//
+// One physical pass splits every segment of the previous pass (rows that
+// share their top c_prev hash bits, stored contiguously) into 2^b
+// sub-buckets on the next b bits.  Three kernels per pass:
+//   k_part_hist    per 4096-row tile: shared-memory histogram of the b-bit
+//                  digit with warp-aggregated atomics (__match_any_sync), one
+//                  count per (segment, digit, tile) written digit-major;
+//   scan_u32       device-wide exclusive scan over those counts, which yields
+//                  every tile's first output row for every digit;
+//   k_part_scatter re-reads the tile, ranks its rows by digit in shared
+//                  memory, and for each column (key first, then payloads of
+//                  1/2/4/8/16 bytes) stages the tile in digit order and writes
+//                  each digit's run contiguously -- the column-first scatter
+//                  of the reference, with the staging done in shared memory so
+//                  stores coalesce.
+// No atomics touch global memory; the output is deterministic.
+#include "internal.h"
+
+namespace phjg
+{
+namespace
+{
+constexpr int kNT = 512;
+constexpr int kRPT = 8;
+constexpr uint32_t kTile = kNT * kRPT; // rows per tile
+constexpr uint32_t kMaxPassBits = 11;  // shared-memory digit histogram <= 2048 bins
+
+struct PassGeom
+{
+    const uint32_t * seg_off;  // n_segs + 1: first row of each input segment
+    const uint32_t * tile_pre; // n_segs + 1: first tile of each input segment
+    uint32_t n_segs;
+    uint32_t shift;            // digit = (hash >> shift) & mask
+    uint32_t b;
+};
+
+struct TileRef
+{
+    uint32_t seg, k, nt, row0, row1, tile0;
+};
+
+__device__ __forceinline__ bool locate_tile(const PassGeom & g, uint32_t t, TileRef & r)
+{
+    const uint32_t total = g.tile_pre[g.n_segs];
+    if (t >= total)
+        return false;
+    // Largest s with tile_pre[s] <= t; segments without tiles are skipped
+    // because then tile_pre[s] == tile_pre[s+1].
+    uint32_t lo = 0, hi = g.n_segs; // invariant: tile_pre[lo] <= t < tile_pre[hi]
+    while (hi - lo > 1)
+    {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (g.tile_pre[mid] <= t)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    r.seg = lo;
+    r.tile0 = g.tile_pre[lo];
+    r.k = t - r.tile0;
+    r.nt = g.tile_pre[lo + 1] - r.tile0;
+    const uint32_t s0 = g.seg_off[lo], s1 = g.seg_off[lo + 1];
+    r.row0 = s0 + r.k * kTile;
+    r.row1 = min(r.row0 + kTile, s1);
+    return true;
+}
+
+// Rank of this row within its digit bin, via one shared atomic per group of
+// lanes holding the same digit.  Invalid rows pass d = 0xFFFFFFFF.
+__device__ __forceinline__ uint32_t warp_agg_rank(uint32_t * bins, uint32_t d)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t peers = __match_any_sync(0xffffffffu, d);
+    const uint32_t leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader && d != 0xFFFFFFFFu)
+        base = atomicAdd(&bins[d], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(kNT) k_part_hist(const uint64_t * __restrict__ keys, PassGeom g, uint32_t * __restrict__ counts)
+{
+    extern __shared__ uint32_t bins[];
+    TileRef tr;
+    if (!locate_tile(g, blockIdx.x, tr))
+        return;
+    const uint32_t nb = 1u << g.b, mask = nb - 1;
+    for (uint32_t i = threadIdx.x; i < nb; i += kNT)
+        bins[i] = 0;
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
+    {
+        const uint32_t row = tr.row0 + j * kNT + threadIdx.x;
+        uint32_t d = 0xFFFFFFFFu;
+        if (row < tr.row1)
+            d = (uint32_t)(int_hash64(__ldcs(keys + row)) >> g.shift) & mask;
+        (void)warp_agg_rank(bins, d);
+    }
+    __syncthreads();
+    const uint64_t base = (uint64_t)tr.tile0 * nb;
+    for (uint32_t d = threadIdx.x; d < nb; d += kNT)
+        counts[base + (uint64_t)d * tr.nt + tr.k] = bins[d];
+}
+
+// Exclusive scan of nb bins in shared memory by kNT threads.
+__device__ __forceinline__ void smem_bins_scan(const uint32_t * bins, uint32_t * excl, uint32_t nb, uint32_t * ws)
+{
+    const uint32_t per = (nb + kNT - 1) / kNT;
+    const uint32_t b0 = threadIdx.x * per;
+    uint32_t local = 0;
+    for (uint32_t i = 0; i < per; ++i)
+        if (b0 + i < nb)
+            local += bins[b0 + i];
+    uint32_t total;
+    uint32_t run = block_excl_scan<kNT>(local, ws, &total);
+    for (uint32_t i = 0; i < per; ++i)
+        if (b0 + i < nb)
+        {
+            excl[b0 + i] = run;
+            run += bins[b0 + i];
+        }
+}
+
+template <class T>
+__device__ __forceinline__ void scatter_column(const T * __restrict__ src, T * __restrict__ dst, T * stage, const uint16_t * sorted_d,
+                                               const uint32_t * excl, const uint32_t * gbase, const uint32_t (&lp)[kRPT], const TileRef & tr)
+{
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
+    {
+        const uint32_t row = tr.row0 + j * kNT + threadIdx.x;
+        if (row < tr.row1)
+            stage[lp[j]] = __ldcs(src + row);
+    }
+    __syncthreads();
+    const uint32_t cnt = tr.row1 - tr.row0;
+    for (uint32_t j = threadIdx.x; j < cnt; j += kNT)
+    {
+        const uint32_t d = sorted_d[j];
+        dst[gbase[d] + (j - excl[d])] = stage[j];
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, const __grid_constant__ PassGeom g, const uint32_t * __restrict__ offs, uint32_t maxw)
+{
+    extern __shared__ __align__(16) uint8_t smem[];
+    TileRef tr;
+    if (!locate_tile(g, blockIdx.x, tr))
+        return;
+    const uint32_t nb = 1u << g.b, mask = nb - 1;
+    uint8_t * stage = smem;
+    uint16_t * sorted_d = reinterpret_cast<uint16_t *>(smem + (size_t)kTile * maxw);
+    uint32_t * bins = reinterpret_cast<uint32_t *>(sorted_d + kTile);
+    uint32_t * excl = bins + nb;
+    uint32_t * gbase = excl + nb;
+    uint32_t * ws = gbase + nb;
+
+    for (uint32_t i = threadIdx.x; i < nb; i += kNT)
+        bins[i] = 0;
+    __syncthreads();
+
+    uint64_t key[kRPT];
+    uint32_t dr[kRPT]; // digit << 16 | rank would overflow for 4096-row tiles; keep apart
+    uint32_t rank[kRPT];
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
+    {
+        const uint32_t row = tr.row0 + j * kNT + threadIdx.x;
+        uint32_t d = 0xFFFFFFFFu;
+        key[j] = 0;
+        if (row < tr.row1)
+        {
+            key[j] = __ldcs(in.keys + row);
+            d = (uint32_t)(int_hash64(key[j]) >> g.shift) & mask;
+        }
+        dr[j] = d;
+        rank[j] = warp_agg_rank(bins, d);
+    }
+    __syncthreads();
+    smem_bins_scan(bins, excl, nb, ws);
+    const uint64_t ebase = (uint64_t)tr.tile0 * nb;
+    for (uint32_t d = threadIdx.x; d < nb; d += kNT)
+        gbase[d] = offs[ebase + (uint64_t)d * tr.nt + tr.k];
+    __syncthreads();
+
+    uint32_t lp[kRPT];
+    uint64_t * stage64 = reinterpret_cast<uint64_t *>(stage);
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
+    {
+        if (dr[j] != 0xFFFFFFFFu)
+        {
+            lp[j] = excl[dr[j]] + rank[j];
+            stage64[lp[j]] = key[j];
+            sorted_d[lp[j]] = (uint16_t)dr[j];
+        }
+        else
+            lp[j] = 0;
+    }
+    __syncthreads();
+    const uint32_t cnt = tr.row1 - tr.row0;
+    for (uint32_t j = threadIdx.x; j < cnt; j += kNT)
+    {
+        const uint32_t d = sorted_d[j];
+        out.keys[gbase[d] + (j - excl[d])] = stage64[j];
+    }
+    __syncthreads();
+
+    for (uint32_t c = 0; c < in.n; ++c)
+    {
+        switch (in.width[c])
+        {
+            case 1:
+                scatter_column<uint8_t>((const uint8_t *)in.col[c], (uint8_t *)out.col[c], stage, sorted_d, excl, gbase, lp, tr);
+                break;
+            case 2:
+                scatter_column<uint16_t>((const uint16_t *)in.col[c], (uint16_t *)out.col[c], (uint16_t *)stage, sorted_d, excl, gbase, lp, tr);
+                break;
+            case 4:
+                scatter_column<uint32_t>((const uint32_t *)in.col[c], (uint32_t *)out.col[c], (uint32_t *)stage, sorted_d, excl, gbase, lp, tr);
+                break;
+            case 8:
+                scatter_column<uint64_t>((const uint64_t *)in.col[c], (uint64_t *)out.col[c], (uint64_t *)stage, sorted_d, excl, gbase, lp, tr);
+                break;
+            default:
+                scatter_column<uint4>((const uint4 *)in.col[c], (uint4 *)out.col[c], (uint4 *)stage, sorted_d, excl, gbase, lp, tr);
+                break;
+        }
+    }
+}
+
+__global__ void k_tiles_per_seg(const uint32_t * __restrict__ seg_off, uint32_t n_segs, uint32_t * __restrict__ nt)
+{
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n_segs)
+        nt[s] = (seg_off[s + 1] - seg_off[s] + kTile - 1) / kTile;
+}
+
+__global__ void k_init_single_seg(uint32_t * seg_off, uint32_t n)
+{
+    seg_off[0] = 0;
+    seg_off[1] = n;
+}
+
+// Output bucket offsets of a pass: bucket (s, d) starts at the scanned
+// offset of its first tile; a segment without tiles is empty and all its
+// buckets start where it starts.
+__global__ void k_bucket_offsets(PassGeom g, const uint32_t * __restrict__ offs, uint32_t n, uint32_t * __restrict__ out_off)
+{
+    const uint32_t nb = 1u << g.b;
+    const uint64_t nbuckets = (uint64_t)g.n_segs * nb;
+    const uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i > nbuckets)
+        return;
+    if (i == nbuckets)
+    {
+        out_off[i] = n;
+        return;
+    }
+    const uint32_t s = (uint32_t)(i >> g.b), d = (uint32_t)(i & (nb - 1));
+    const uint32_t t0 = g.tile_pre[s], nt = g.tile_pre[s + 1] - t0;
+    out_off[i] = nt ? offs[(uint64_t)t0 * nb + (uint64_t)d * nt] : g.seg_off[s];
+}
+} // namespace
+
+void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, const std::vector<uint32_t> & pass_bits, const Cols & out,
+                     const Cols & tmp, uint32_t * leaf_off, const char * phase)
+{
+    uint32_t total_bits = 0;
+    std::vector<uint32_t> phys; // physical passes
+    for (uint32_t b : pass_bits)
+    {
+        total_bits += b;
+        const uint32_t pieces = (b + kMaxPassBits - 1) / kMaxPassBits;
+        for (uint32_t p = 0; p < pieces; ++p)
+            phys.push_back(b / pieces + (p < b % pieces ? 1u : 0u));
+    }
+    if (total_bits == 0 || total_bits > 24)
+        throw Error(PHJ_ERR_UNSUPPORTED, "device radix partitioning supports 1..24 total bits");
+    if (n >= (1ull << 32))
+        throw Error(PHJ_ERR_UNSUPPORTED, "device radix partitioning supports < 2^32 rows per side");
+    const uint64_t n_leaves = 1ull << total_bits;
+    if (n == 0)
+    {
+        PHJ_CUDA(cudaMemsetAsync(leaf_off, 0, (n_leaves + 1) * sizeof(uint32_t), ctx->stream));
+        return;
+    }
+    const uint32_t maxw = max_width(in) < 8 ? 8 : max_width(in);
+
+    // Segments of the first pass: the whole input.
+    uint32_t * seg_off = s.get<uint32_t>(2);
+    k_init_single_seg<<<1, 1, 0, ctx->stream>>>(seg_off, (uint32_t)n);
+    PHJ_LAUNCHED(ctx, "part_init");
+    uint32_t n_segs = 1, consumed = 0;
+    const size_t np = phys.size();
+    Cols src = in;
+    for (size_t p = 0; p < np; ++p)
+    {
+        const uint32_t b = phys[p];
+        const uint32_t nb = 1u << b;
+        const Cols & dst = ((np - 1 - p) % 2 == 0) ? out : tmp;
+        // Tiles of each segment, then their prefix.
+        uint32_t * nt = s.get<uint32_t>(n_segs + 1);
+        k_tiles_per_seg<<<(unsigned)ceil_div(n_segs, 256), 256, 0, ctx->stream>>>(seg_off, n_segs, nt);
+        PHJ_LAUNCHED(ctx, "part_tiles");
+        uint32_t * tile_pre = s.get<uint32_t>(n_segs + 1);
+        scan_u32(ctx, s, nt, tile_pre, n_segs);
+        const uint64_t tiles_ub = ceil_div(n, kTile) + n_segs;
+        const uint64_t entries_ub = tiles_ub * nb;
+        // Entries past the real tile count stay unwritten; they only follow
+        // the real ones in the scan, so they cannot disturb real offsets.
+        uint32_t * counts = s.get<uint32_t>(entries_ub + 1);
+        const PassGeom g{seg_off, tile_pre, n_segs, 64u - consumed - b, b};
+        {
+            KTimer kt(ctx, "part_hist", n, n * 8);
+            k_part_hist<<<(unsigned)tiles_ub, kNT, nb * sizeof(uint32_t), ctx->stream>>>(src.keys, g, counts);
+            PHJ_LAUNCHED(ctx, "part_hist");
+        }
+        scan_u32(ctx, s, counts, counts, entries_ub);
+        {
+            const size_t smem = (size_t)kTile * maxw + (size_t)kTile * sizeof(uint16_t) + 3ull * nb * sizeof(uint32_t) + 32 * sizeof(uint32_t);
+            uint64_t row_bytes = 8;
+            for (uint32_t c = 0; c < in.n; ++c)
+                row_bytes += in.width[c];
+            KTimer kt(ctx, phase, n, 2 * n * row_bytes);
+            k_part_scatter<<<(unsigned)tiles_ub, kNT, smem, ctx->stream>>>(src, dst, g, counts, maxw);
+            PHJ_LAUNCHED(ctx, "part_scatter");
+        }
+        const uint64_t nbuckets = (uint64_t)n_segs * nb;
+        uint32_t * next_off = (p + 1 == np) ? leaf_off : s.get<uint32_t>(nbuckets + 1);
+        k_bucket_offsets<<<(unsigned)ceil_div(nbuckets + 1, 256), 256, 0, ctx->stream>>>(g, counts, (uint32_t)n, next_off);
+        PHJ_LAUNCHED(ctx, "part_offsets");
+        seg_off = next_off;
+        n_segs = (uint32_t)nbuckets;
+        consumed += b;
+        src = dst;
+    }
+}
+
+void set_partition_smem_limits(int smem_optin)
+{
+    // The scatter kernel stages a 4096-row tile of the widest column (<= 16
+    // bytes) plus digit bins: up to ~96 KiB.
+    const size_t need = (size_t)kTile * 16 + (size_t)kTile * sizeof(uint16_t) + 3ull * (1u << kMaxPassBits) * sizeof(uint32_t) + 128;
+    PHJ_CUDA(cudaFuncSetAttribute(k_part_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin)));
+}
+
+} // namespace phjg

@@ -1,0 +1,72 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, it
+exports every function include/phj_gpu.h declares, and the radix
+configuration resolves as the reference CLI does (src/CLI.cpp:376-408)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+import phj_gpu as P
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in os.listdir(os.path.join(ROOT, "include")):
+        if h.endswith(".h"):
+            text = open(os.path.join(ROOT, "include", h)).read()
+            text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+            names |= set(re.findall(r"\b(phj_[a-z0-9_]+)\s*\(", text))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    if not os.path.exists(P.LIB_PATH):
+        import subprocess
+        subprocess.run(["make", "-s", "-j4", "-C", os.path.join(ROOT, "phj-bench_gb300")], check=True)
+    return P.load()
+
+
+def test_library_exports_every_declared_symbol(lib):
+    names = declared_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_abi_version(lib):
+    assert lib.phj_abi_version() == 1
+
+
+@pytest.mark.parametrize("parts,passes,want", [
+    (256, 1, [8]), (65536, 2, [8, 8]), (262144, 3, [6, 6, 6]), (1024, 3, [4, 3, 3]), (2, 1, [1]), (1 << 32, 2, [16, 16]),
+])
+def test_resolve_radix_matches_cli(lib, parts, passes, want):
+    assert P.resolve_radix(parts, passes) == want
+
+
+def test_resolve_radix_bits_override(lib):
+    assert P.resolve_radix(bits_per_pass=[6, 4]) == [6, 4]
+
+
+@pytest.mark.parametrize("parts,passes,bits", [(100, 1, None), (256, 9, None), (0, 0, [0]), (0, 0, [17]), (0, 0, [16, 16, 1])])
+def test_resolve_radix_rejects_what_the_cli_rejects(lib, parts, passes, bits):
+    with pytest.raises(P.PhjError):
+        P.resolve_radix(parts, passes, bits)
+
+
+def test_context_without_a_device_reports_no_device(lib):
+    try:
+        import subprocess
+        has_gpu = subprocess.run(["nvidia-smi", "-L"], capture_output=True).returncode == 0
+    except FileNotFoundError:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    p = ctypes.c_void_p()
+    assert lib.phj_ctx_create(0, ctypes.byref(p)) == 6  # PHJ_ERR_NO_DEVICE
+    with pytest.raises(P.PhjError):
+        P.Context(0)
