@@ -1,0 +1,412 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 hash-join path (one JSON line on stdout).
+
+Default workload (the 16M x 256M uint64 join the headline metric is quoted
+on): build side 16M rows of unique splitmix64 keys with u64 and u32 payloads,
+probe side 256M rows whose keys are drawn uniformly from the build keys with
+10% replaced by non-matching keys, one u64 payload; radix 2 passes x 8 bits
+(65,536 leaves); scheme PHJ-PURE (runPHJ).  Inputs are generated on the
+device (seeded, synthetic) and are resident in HBM before timing.
+
+  value  build+probe tuples/s of the join with inputs resident in HBM
+         (CUDA events on the library's stream around each join);
+  e2e    the same metric through the C ABI with HOST (pinned) inputs and
+         outputs: upload, join, and download of the result inside the timing;
+  roofline  the dominant kernel's algorithmic bytes per launch over its
+         CUDA-event duration, against the measured HBM copy bandwidth;
+  cpu_baseline  the reference's PHJ-PURE on the host cores (its C++ port in
+         oracle/, since the reference sources are not on this machine) over a
+         bounded sample of the same workload.
+
+--impl reference runs only that CPU implementation, as the reference arm.
+Multi-GPU: the join does not exchange data between GPUs here, so N ranks run
+N independent replicas (weak scaling) with a barrier and max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "phj-bench_gb300"), os.path.join(ROOT, "oracle")]
+
+import numpy as np  # noqa: E402
+
+M = 1 << 20
+WIDTH = {0: 1, 1: 2, 2: 4, 3: 8, 4: 16}
+
+WORKLOADS = {
+    # name: (description, scheme, build spec, probe spec, radix bits)
+    "c2": ("PHJ-PURE 16M x 256M: unique splitmix64 u64 build keys with u64,u32 payloads; probe keys uniform from the build "
+           "keys with 10% non-matching, u64 payload; 2 passes x 8 bits (65,536 leaves)", "phj-pure",
+           dict(kind=0, rows=16 * M, seed=0xB1, key_seed=0x5EED, types=[3, 2]),
+           dict(kind=4, rows=256 * M, seed=0xB2, key_seed=0x5EED, types=[3], domain=16 * M, match_permille=900), [8, 8]),
+    "c1": ("PHJ-PURE 1M x 8M: build keys a permutation of 1..1M with a u64 payload; probe keys uniform over 1..1M with a "
+           "u32 payload; 1 pass x 8 bits", "phj-pure",
+           dict(kind=1, rows=1 * M, seed=0xC1, key_seed=0, types=[3]),
+           dict(kind=3, rows=8 * M, seed=0xC2, key_seed=0, types=[2], domain=1 * M), [8]),
+    "c3": ("PHJ-PURE multi-match 32M x 128M: ~8M distinct build keys, geometric multiplicity (mean ~4, cap 16), u8,u16,u128 "
+           "payloads; probe 50% from the distinct build keys, u32 payload; 2 passes x 8 bits", "phj-pure",
+           dict(kind=2, rows=32 * M, seed=0xD1, key_seed=0x77, types=[0, 1, 4]),
+           dict(kind=4, rows=128 * M, seed=0xD2, key_seed=0x77, types=[2], domain=None, match_permille=500), [8, 8]),
+}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class Dist:
+    """Barrier and max-reduce across ranks (gloo on CPU tensors) when N > 1."""
+
+    def __init__(self, world):
+        self.world = world
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist:
+            self.dist.barrier()
+
+    def max(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, x):
+        if not self.dist:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join("/tmp", f"phj_clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except FileNotFoundError:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured copy bandwidth (MEASURED_PEAKS.json, burst)"
+    except Exception:
+        return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
+
+
+def profiled_traffic(kernel, workload):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        e = d.get(workload, {}).get(kernel)
+        return e["dram_bytes_per_launch"] if e else None
+    except Exception:
+        return None
+
+
+def row_bytes(types):
+    return 8 + sum(WIDTH[t] for t in types)
+
+
+def make_tables(ctx, wl):
+    _, _, bspec, pspec, _ = WORKLOADS[wl]
+    b = ctx.generate(bspec["kind"], bspec["rows"], bspec["seed"], bspec["key_seed"], bspec["types"])
+    pspec = dict(pspec)
+    if pspec.get("domain") is None:
+        pspec["domain"] = b.gen_distinct
+    p = ctx.generate(pspec["kind"], pspec["rows"], pspec["seed"], pspec["key_seed"], pspec["types"], domain=pspec["domain"],
+                     match_permille=pspec.get("match_permille", 1000))
+    return b, p
+
+
+def scale_workload(name, f):
+    desc, scheme, bspec, pspec, bits = WORKLOADS[name]
+    bspec, pspec = dict(bspec), dict(pspec)
+    bspec["rows"] = max(1, int(bspec["rows"] * f))
+    pspec["rows"] = max(1, int(pspec["rows"] * f))
+    if pspec.get("domain") and bspec["kind"] in (0, 1):
+        pspec["domain"] = bspec["rows"]
+    WORKLOADS[name] = (f"{desc} [rows scaled by {f:g}]", scheme, bspec, pspec, bits)
+
+
+def run_scheme(ctx, scheme, b, p, bits):
+    if scheme == "chj":
+        return ctx.run_chj(b, p)
+    return ctx.run_phj_pure(b, p, bits)
+
+
+def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3):
+    import oracle
+    n_p = max(1, int(len(phost.keys) * frac))
+    probe = type(phost)(phost.types, phost.keys[:n_p], [c[:n_p] for c in phost.payloads])
+    times = []
+    for _ in range(reps):
+        _, ms = oracle.port_run(scheme, bhost, probe, bits, threads)
+        times.append(ms["e2e"])
+    t = statistics.median(times) / 1e3
+    return {"value": (len(bhost.keys) + n_p) / t, "unit": "tuples/s", "cores": threads, "kind": "port",
+            "sample": f"{scheme} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
+                      f"({frac:.4g} of the probe side); median of {reps} runs, {threads} host threads; "
+                      f"C++ port of the reference's scheme (oracle/cpu_port.cpp)",
+            "ms_per_run": statistics.median(times)}
+
+
+def host_streams_from_device(ctx, b, p):
+    return b.download(), p.download()
+
+
+def reference_arm(args, rank, world, dist):
+    """The reference's CPU implementation (its C++ port) on the host cores."""
+    if rank != 0:
+        return
+    import oracle
+    import phj_datagen as G
+    import phj_gpu as P
+    desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    frac = args.cpu_probe_frac
+    if bspec["kind"] == 2:
+        bk, used = G.gen_multi_match_keys(bspec["rows"], bspec["seed"], bspec["key_seed"])
+    else:
+        bk, used = G.gen_keys(bspec["kind"], bspec["rows"], bspec["seed"], bspec["key_seed"]), bspec["rows"]
+    b = P.BlockStream(bspec["types"], bk, G.payload_columns(bspec["seed"], bspec["types"], bspec["rows"]))
+    n_p = max(1, int(pspec["rows"] * frac))
+    dom = pspec.get("domain") or used
+    if pspec["kind"] == 4:
+        pk = G.gen_keys(4, n_p, pspec["seed"], pspec["key_seed"], domain=dom, match_permille=pspec["match_permille"])
+    else:
+        pk = G.gen_keys(pspec["kind"], n_p, pspec["seed"], pspec["key_seed"], domain=dom)
+    p = P.BlockStream(pspec["types"], pk, G.payload_columns(pspec["seed"], pspec["types"], n_p))
+    for _ in range(args.warmup):
+        oracle.port_run(scheme, b, p, bits, threads)
+    times = []
+    for _ in range(args.steps):
+        _, ms = oracle.port_run(scheme, b, p, bits, threads)
+        times.append(ms["e2e"])
+    t = statistics.mean(times)
+    value = (len(b.keys) + n_p) / (t / 1e3)
+    line = {
+        "impl": "reference", "metric": "join tuples/s (build+probe)", "value": value, "unit": "tuples/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded, same generator specification as the GPU arm)",
+        "config": {"workload": desc, "scheme": scheme, "build_rows": len(b.keys), "probe_rows": n_p,
+                   "probe_sample_of": pspec["rows"], "radix_pass_bits": bits},
+        "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": threads, "kind": "port",
+                         "sample": f"full build side, first {n_p} of {pspec['rows']} probe rows; C++ port of the reference's "
+                                   f"{scheme} (oracle/cpu_port.cpp) because the reference sources are not on this machine"},
+        "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--scheme", default=None, choices=["phj-pure", "chj"])
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--cpu-probe-frac", type=float, default=1 / 16)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-chj", action="store_true")
+    ap.add_argument("--scale", type=float, default=1.0, help="multiply both sides' rows (profiling on a smaller case)")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    dist = Dist(world)
+    if args.impl == "reference":
+        reference_arm(args, rank, world, dist)
+        return
+
+    import phj_gpu as P
+    desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
+    scheme = args.scheme or scheme
+    if args.scale != 1.0:
+        scale_workload(args.workload, args.scale)
+        desc, _, bspec, pspec, _ = WORKLOADS[args.workload]
+    ctx = P.Context(local)
+    b, p = make_tables(ctx, args.workload)
+    B, Pn = b.rows, p.rows
+    tuples = B + Pn
+
+    # -------- device-resident timing --------
+    sampler = ClockSampler(local)
+    for _ in range(args.warmup):
+        out, _ = run_scheme(ctx, scheme, b, p, bits)
+        out.free()
+    sampler.start()
+    dist.barrier()
+    launches0 = ctx.launch_count()
+    step_ms, kernel_runs, out_rows = [], [], 0
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.flush_l2()
+        out, res = run_scheme(ctx, scheme, b, p, bits)
+        step_ms.append(res.e2e_wall_ms)
+        kernel_runs.append(ctx.kernel_times())
+        out_rows = out.rows
+        if _ == args.steps - 1:
+            launches = ctx.launch_count() - launches0  # joins only (the L2 flush is a memset)
+            fp_main = out.fingerprint()
+        out.free()
+    wall = time.perf_counter() - t_wall0
+    dist.barrier()
+    clocks = sampler.stop()
+    ms_per_step = dist.max(statistics.mean(step_ms))
+    total_tuples = dist.sum(tuples)
+    value = total_tuples / (ms_per_step / 1e3)
+
+    # dominant kernel: largest mean time per step, then its per-launch average
+    per_name = {}
+    for run in kernel_runs:
+        for k in run:
+            d = per_name.setdefault(k["name"], {"ms": 0.0, "launches": 0, "bytes": 0})
+            d["ms"] += k["ms"]
+            d["launches"] += 1
+            d["bytes"] += k["bytes"]
+    dom_name = max(per_name, key=lambda n: per_name[n]["ms"])
+    dom = per_name[dom_name]
+    peak, peak_src = measured_peak()
+    avg_ms = dom["ms"] / dom["launches"]
+    bytes_per_launch = dom["bytes"] / dom["launches"]
+    achieved = bytes_per_launch / (avg_ms / 1e3) / 1e9
+    bmin = B * row_bytes(bspec["types"]) + Pn * row_bytes(pspec["types"]) + out_rows * (
+        8 + sum(WIDTH[t] for t in bspec["types"]) + sum(WIDTH[t] for t in pspec["types"]))
+    join_gbs = bmin / (statistics.mean(step_ms) / 1e3) / 1e9
+    kernel_share = {n: round(d["ms"] / sum(x["ms"] for x in per_name.values()), 4) for n, d in
+                    sorted(per_name.items(), key=lambda kv: -kv[1]["ms"])}
+
+    line = {
+        "metric": "join tuples/s (build+probe)", "value": value, "unit": "tuples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64", "data": "synthetic (seeded device generator; keys, payloads and match rate as specified)",
+        "config": {"workload": desc, "scheme": scheme, "build_rows": B, "probe_rows": Pn, "radix_pass_bits": bits,
+                   "output_rows": out_rows, "l2": "inputs larger than L2 (probe side 4.3 GB) and an L2 flush between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload),
+                     "bytes_per_launch": bytes_per_launch, "ms_per_launch": avg_ms, "peak_source": peak_src},
+        "join_roofline": {"bytes_min": bmin, "achieved_gbs": join_gbs, "frac": join_gbs / peak,
+                          "definition": "B*(8+sum w_b) + P*(8+sum w_p) + O*(8+sum w_b+sum w_p) over the join's device time"},
+        "kernel_share": kernel_share,
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "wall_s_timed": wall,
+        "fingerprint": [str(v) for v in fp_main],
+    }
+
+    # -------- CHJ on the same inputs (extra line item) --------
+    if not args.no_chj and scheme != "chj":
+        for _ in range(2):
+            out, _ = ctx.run_chj(b, p)
+            out.free()
+        cms = []
+        for _ in range(max(3, args.steps // 2)):
+            ctx.flush_l2()
+            out, res = ctx.run_chj(b, p)
+            cms.append(res.e2e_wall_ms)
+            fp_chj = out.fingerprint()
+            out.free()
+        line["chj"] = {"value": tuples / (statistics.mean(cms) / 1e3), "ms_per_step": statistics.mean(cms),
+                       "fingerprint_equals_phj_pure": fp_chj == fp_main}
+
+    hb = hp = None
+    if not (args.no_e2e and (args.no_cpu or rank != 0 or world != 1)):
+        hb, hp = host_streams_from_device(ctx, b, p)
+    # -------- end to end through the C ABI with host buffers --------
+    if not args.no_e2e:
+        pin = []
+        for s in (hb, hp):
+            keys = ctx.pinned((len(s.keys),), np.uint64)
+            keys[:] = s.keys
+            cols = []
+            for c in s.payloads:
+                a = ctx.pinned(c.shape, c.dtype)
+                a[...] = c
+                cols.append(a)
+            pin.append(P.BlockStream(s.types, keys, cols, block_rows=s.block_rows))
+        cap = out_rows
+        okeys = ctx.pinned((cap,), np.uint64)
+        oleft = [ctx.pinned((cap, 2), np.uint64) if t == 4 else ctx.pinned((cap,), P.TYPE_DTYPE[t]) for t in bspec["types"]]
+        oright = [ctx.pinned((cap, 2), np.uint64) if t == 4 else ctx.pinned((cap,), P.TYPE_DTYPE[t]) for t in pspec["types"]]
+        h2d = sum(s.keys.nbytes + sum(c.nbytes for c in s.payloads) for s in pin)
+        d2h = out_rows * (8 + sum(WIDTH[t] for t in bspec["types"]) + sum(WIDTH[t] for t in pspec["types"]))
+        e2e_t = []
+        for i in range(args.e2e_steps + 1):
+            dist.barrier()
+            t0 = time.perf_counter()
+            tb, tp = ctx.upload(pin[0]), ctx.upload(pin[1])
+            out, _ = run_scheme(ctx, scheme, tb, tp, bits)
+            out.download((okeys, oleft, oright))
+            t1 = time.perf_counter()
+            out.free(), tb.free(), tp.free()
+            if i > 0:  # first one warms the host paths
+                e2e_t.append(t1 - t0)
+        e2e_s = dist.max(statistics.mean(e2e_t))
+        line["e2e"] = {"value": total_tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                       "ms_per_step": e2e_s * 1e3}
+        del pin
+
+    # -------- CPU baseline (rank 0, N = 1 only) --------
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            line["cpu_baseline"] = cpu_baseline(hb, hp, bits, args.cpu_probe_frac, os.cpu_count() or 1, scheme)
+        except Exception as e:  # the baseline is reported, never the target
+            line["cpu_baseline"] = {"value": None, "error": str(e)}
+    b.free(), p.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -234,3 +234,67 @@ def ref_run_scheme(scheme: int, build, probe, pass_bits, threads: int = 4, budge
                                out.ctypes.data, max(n, 1), w, stats)
     assert got >= 0, got
     return out[:got], list(stats)
+
+
+# ---- the CPU port of the reference's schemes (cpu_port.cpp) -----------------
+
+class PortStream(C.Structure):
+    _fields_ = [("rows", C.c_uint64), ("keys", C.c_void_p), ("n_payloads", C.c_uint32), ("types", C.c_uint8 * 8),
+                ("cols", C.c_void_p * 8), ("block_rows", C.c_uint32)]
+
+
+_port = None
+
+
+def port():
+    global _port
+    if _port is None:
+        path = os.path.join(HERE, "libcpuport.so")
+        if not os.path.exists(path):
+            subprocess.run(["make", "-s", "-C", HERE, "libcpuport.so"], check=True)
+        L = C.CDLL(path)
+        S = C.POINTER(PortStream)
+        L.port_run_phj_pure.restype = C.c_int64
+        L.port_run_phj_pure.argtypes = [S, S, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]
+        L.port_run_chj.restype = C.c_int64
+        L.port_run_chj.argtypes = [S, S, C.c_uint32, C.POINTER(C.c_double)]
+        _port = L
+    return _port
+
+
+def port_stream(s, block_rows: int = 10_000) -> PortStream:
+    o = PortStream()
+    o.rows = len(s.keys)
+    o.keys = s.keys.ctypes.data if len(s.keys) else None
+    o.n_payloads = len(s.types)
+    for i, (t, p) in enumerate(zip(s.types, s.payloads)):
+        o.types[i] = t
+        o.cols[i] = p.ctypes.data if len(s.keys) else None
+    o.block_rows = block_rows
+    o._keep = s
+    return o
+
+
+def port_run(scheme: str, build, probe, pass_bits=(8,), threads: int = 0):
+    """Times the CPU port of the reference's runPHJ ('phj-pure') or runCHJ
+    ('chj').  Returns (output rows, phase ms dict)."""
+    threads = threads or (os.cpu_count() or 1)
+    ms = (C.c_double * 5)()
+    b, p = port_stream(build), port_stream(probe)
+    if scheme == "phj-pure":
+        bits = (C.c_uint8 * len(pass_bits))(*pass_bits)
+        n = port().port_run_phj_pure(C.byref(b), C.byref(p), bits, len(pass_bits), threads, ms)
+        return n, {"build_shuffle": ms[0], "build": ms[1], "probe_shuffle": ms[2], "probe": ms[3], "e2e": ms[4]}
+    n = port().port_run_chj(C.byref(b), C.byref(p), threads, ms)
+    return n, {"build": ms[0], "probe": ms[1], "e2e": ms[2]}
+
+
+def ref_time(scheme: str, build, probe, pass_bits=(8,), threads: int = 0, budget_mib: int = 512):
+    """Times the reference itself (only where it was compiled)."""
+    threads = threads or (os.cpu_count() or 1)
+    code = {"chj": 0, "phj-pure": 1, "phj": 2}[scheme]
+    b, p = ostream(build), ostream(probe)
+    bits = (C.c_uint8 * len(pass_bits))(*pass_bits)
+    rows = C.c_uint64()
+    ms = ref().ref_time_scheme(code, C.byref(b), C.byref(p), 10_000, bits, len(pass_bits), threads, budget_mib, C.byref(rows))
+    return rows.value, ms
