@@ -413,6 +413,7 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     a.block_off = B.block_off;
     a.uniform_block_rows = B.uniform_block_rows;
     a.any_dup = lt.any_dup;
+    a.uniform_log2cap = -1;
     phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(e2));
@@ -477,6 +478,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     a.leaf_bits = total_bits;
     a.chj = 0;
     a.any_dup = lt.any_dup;
+    a.uniform_log2cap = lt.uniform_log2cap;
     phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(ev[4]));

@@ -37,25 +37,32 @@ __device__ __forceinline__ uint32_t log2u(uint64_t x)
     return 63u - (uint32_t)__clzll((long long)x);
 }
 
+// One CTA per leaf.  Tables are either uniform (every leaf 2^ulog cells at
+// leaf << ulog, ulog >= 0) or sized per leaf through table_off (ulog < 0).
+// The RowRefCell of a build row is {0, row}: block 0 is the whole
+// leaf-partitioned build side, row its index there.
 __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __restrict__ keys, const uint32_t * __restrict__ leaf_off,
-                                                         const uint32_t * __restrict__ table_off, uint32_t smem_cells, Cell * __restrict__ cells,
-                                                         uint64_t * __restrict__ next, LeafMeta * __restrict__ meta, int * __restrict__ any_dup)
+                                                         const uint32_t * __restrict__ table_off, int ulog, uint32_t smem_cells,
+                                                         Cell * __restrict__ cells, uint64_t * __restrict__ next, LeafMeta * __restrict__ meta,
+                                                         int * __restrict__ any_dup)
 {
     extern __shared__ __align__(16) Cell sh_cells[];
     __shared__ int dup;
     const uint32_t l = blockIdx.x;
     const uint32_t r0 = leaf_off[l], r = leaf_off[l + 1] - r0;
-    const uint64_t t0 = table_off[l];
-    const uint64_t cap = table_off[l + 1] - t0;
+    const uint64_t t0 = ulog >= 0 ? ((uint64_t)l << ulog) : table_off[l];
+    const uint64_t cap = ulog >= 0 ? (1ull << ulog) : table_off[l + 1] - t0;
     if (threadIdx.x == 0)
         dup = 0;
+    const Cell empty{0ull, INVALID_REF};
     if (r == 0)
     {
+        for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT) // uniform layout: an empty table
+            reinterpret_cast<ulonglong2 *>(cells + t0)[i] = make_ulonglong2(0ull, INVALID_REF);
         if (threadIdx.x == 0)
-            meta[l] = LeafMeta{t0, r0, 0, 0, 0, 0};
+            meta[l] = LeafMeta{t0, r0, cap ? (uint8_t)log2u(cap) : (uint8_t)0, 0, 0, 0};
         return;
     }
-    const Cell empty{0ull, INVALID_REF};
     const bool in_smem = cap <= smem_cells;
     Cell * tab = in_smem ? sh_cells : cells + t0;
     for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT)
@@ -66,7 +73,7 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
     {
         const uint64_t k = keys[r0 + i];
         const uint64_t h = int_hash64(k);
-        const uint64_t ref = make_ref(l, i);
+        const uint64_t ref = make_ref(0, r0 + i);
         const uint64_t prev = in_smem ? table_insert<true>(tab, cap, h, k, ref) : table_insert<false>(tab, cap, h, k, ref);
         next[r0 + i] = prev;
         my_dup |= ref_valid(prev);
@@ -180,16 +187,22 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     PHJ_CUDA(cudaMemcpyAsync(&host[1], table_off + n_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
     lt.max_rows = host[0];
-    lt.total_cells = host[1];
+    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
+    // Uniform capacity (the largest leaf's) lets the probe compute a table's
+    // address from the leaf id alone; it is used unless it costs more than
+    // 1.5x the cells of per-leaf sizing.
+    const uint64_t uniform_cells = (uint64_t)n_leaves * max_cap;
+    const bool uniform = uniform_cells <= (3 * (uint64_t)host[1]) / 2 + n_leaves;
+    lt.uniform_log2cap = uniform ? (int)(63 - __builtin_clzll(max_cap)) : -1;
+    lt.total_cells = uniform ? uniform_cells : host[1];
     lt.meta = s.get<LeafMeta>(n_leaves);
     lt.cells = s.get<Cell>(lt.total_cells);
-    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
     const uint32_t smem_cells = (uint32_t)std::min<uint64_t>(max_cap, kSmemCellsMax);
     int * any_dup = reinterpret_cast<int *>(small + 1);
     {
         KTimer kt(ctx, "build_leaf_tables", 0, 0);
-        k_build_leaf<<<n_leaves, kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, smem_cells, lt.cells,
-                                                                                            lt.next, lt.meta, any_dup);
+        k_build_leaf<<<n_leaves, kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, lt.uniform_log2cap,
+                                                                                            smem_cells, lt.cells, lt.next, lt.meta, any_dup);
         PHJ_LAUNCHED(ctx, "build_leaf");
     }
     PHJ_CUDA(cudaMemcpyAsync(&lt.any_dup, any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -199,6 +199,7 @@ struct LeafTables
     uint64_t total_cells = 0;
     uint32_t max_rows = 0;
     int any_dup = 0;
+    int uniform_log2cap = -1; // >= 0: every leaf table has 2^this cells at leaf << this
 };
 
 // Per-leaf tables over leaf-partitioned build rows (PHJ-PURE / PHJ).
@@ -221,6 +222,7 @@ struct ProbeArgs
     const uint64_t * block_off;
     uint32_t uniform_block_rows;
     int any_dup;
+    int uniform_log2cap;    // >= 0: PHJ leaf tables of uniform capacity (no directory lookup)
 };
 // Returns the number of output rows; writes them to `out` unless count_only.
 uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name);

@@ -6,8 +6,8 @@
 // share their top c_prev hash bits, stored contiguously) into 2^b
 // sub-buckets on the next b bits.  Three kernels per pass:
 //   k_part_hist    per 4096-row tile: shared-memory histogram of the b-bit
-//                  digit with warp-aggregated atomics (__match_any_sync), one
-//                  count per (segment, digit, tile) written digit-major;
+//                  digit, one count per (segment, digit, tile) written
+//                  digit-major;
 //   scan_u32       device-wide exclusive scan over those counts, which yields
 //                  every tile's first output row for every digit;
 //   k_part_scatter re-reads the tile, ranks its rows by digit in shared
@@ -68,19 +68,6 @@ __device__ __forceinline__ bool locate_tile(const PassGeom & g, uint32_t t, Tile
     return true;
 }
 
-// Rank of this row within its digit bin, via one shared atomic per group of
-// lanes holding the same digit.  Invalid rows pass d = 0xFFFFFFFF.
-__device__ __forceinline__ uint32_t warp_agg_rank(uint32_t * bins, uint32_t d)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t peers = __match_any_sync(0xffffffffu, d);
-    const uint32_t leader = __ffs(peers) - 1;
-    uint32_t base = 0;
-    if (lane == leader && d != 0xFFFFFFFFu)
-        base = atomicAdd(&bins[d], (uint32_t)__popc(peers));
-    base = __shfl_sync(peers, base, leader);
-    return base + __popc(peers & ((1u << lane) - 1u));
-}
 
 __global__ void __launch_bounds__(kNT) k_part_hist(const uint64_t * __restrict__ keys, PassGeom g, uint32_t * __restrict__ counts)
 {
@@ -96,10 +83,8 @@ __global__ void __launch_bounds__(kNT) k_part_hist(const uint64_t * __restrict__
     for (int j = 0; j < kRPT; ++j)
     {
         const uint32_t row = tr.row0 + j * kNT + threadIdx.x;
-        uint32_t d = 0xFFFFFFFFu;
         if (row < tr.row1)
-            d = (uint32_t)(int_hash64(__ldcs(keys + row)) >> g.shift) & mask;
-        (void)warp_agg_rank(bins, d);
+            atomicAdd(&bins[(uint32_t)(int_hash64(__ldcs(keys + row)) >> g.shift) & mask], 1u);
     }
     __syncthreads();
     const uint64_t base = (uint64_t)tr.tile0 * nb;
@@ -126,9 +111,11 @@ __device__ __forceinline__ void smem_bins_scan(const uint32_t * bins, uint32_t *
         }
 }
 
+// One column of the tile: stage it in digit order in shared memory, then
+// each thread stores its kRPT staged elements to their precomputed rows.
 template <class T>
-__device__ __forceinline__ void scatter_column(const T * __restrict__ src, T * __restrict__ dst, T * stage, const uint16_t * sorted_d,
-                                               const uint32_t * excl, const uint32_t * gbase, const uint32_t (&lp)[kRPT], const TileRef & tr)
+__device__ __forceinline__ void scatter_column(const T * __restrict__ src, T * __restrict__ dst, T * stage, const uint32_t (&lp)[kRPT],
+                                               const uint32_t (&dest)[kRPT], const TileRef & tr)
 {
 #pragma unroll
     for (int j = 0; j < kRPT; ++j)
@@ -139,15 +126,18 @@ __device__ __forceinline__ void scatter_column(const T * __restrict__ src, T * _
     }
     __syncthreads();
     const uint32_t cnt = tr.row1 - tr.row0;
-    for (uint32_t j = threadIdx.x; j < cnt; j += kNT)
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
     {
-        const uint32_t d = sorted_d[j];
-        dst[gbase[d] + (j - excl[d])] = stage[j];
+        const uint32_t pos = j * kNT + threadIdx.x;
+        if (pos < cnt)
+            dst[dest[j]] = stage[pos];
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, const __grid_constant__ PassGeom g, const uint32_t * __restrict__ offs, uint32_t maxw)
+__global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out,
+                                                         const __grid_constant__ PassGeom g, const uint32_t * __restrict__ offs, uint32_t maxw)
 {
     extern __shared__ __align__(16) uint8_t smem[];
     TileRef tr;
@@ -165,22 +155,23 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
         bins[i] = 0;
     __syncthreads();
 
+    // digit and rank within the digit (shared atomics return the rank)
     uint64_t key[kRPT];
-    uint32_t dr[kRPT]; // digit << 16 | rank would overflow for 4096-row tiles; keep apart
+    uint32_t lp[kRPT]; // digit, then position in the tile's digit order
     uint32_t rank[kRPT];
 #pragma unroll
     for (int j = 0; j < kRPT; ++j)
     {
         const uint32_t row = tr.row0 + j * kNT + threadIdx.x;
-        uint32_t d = 0xFFFFFFFFu;
+        lp[j] = 0xFFFFFFFFu;
         key[j] = 0;
+        rank[j] = 0;
         if (row < tr.row1)
         {
             key[j] = __ldcs(in.keys + row);
-            d = (uint32_t)(int_hash64(key[j]) >> g.shift) & mask;
+            lp[j] = (uint32_t)(int_hash64(key[j]) >> g.shift) & mask;
+            rank[j] = atomicAdd(&bins[lp[j]], 1u);
         }
-        dr[j] = d;
-        rank[j] = warp_agg_rank(bins, d);
     }
     __syncthreads();
     smem_bins_scan(bins, excl, nb, ws);
@@ -189,26 +180,33 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
         gbase[d] = offs[ebase + (uint64_t)d * tr.nt + tr.k];
     __syncthreads();
 
-    uint32_t lp[kRPT];
     uint64_t * stage64 = reinterpret_cast<uint64_t *>(stage);
 #pragma unroll
     for (int j = 0; j < kRPT; ++j)
-    {
-        if (dr[j] != 0xFFFFFFFFu)
+        if (lp[j] != 0xFFFFFFFFu)
         {
-            lp[j] = excl[dr[j]] + rank[j];
+            const uint32_t d = lp[j];
+            lp[j] = excl[d] + rank[j];
             stage64[lp[j]] = key[j];
-            sorted_d[lp[j]] = (uint16_t)dr[j];
+            sorted_d[lp[j]] = (uint16_t)d;
         }
         else
             lp[j] = 0;
-    }
     __syncthreads();
+    // Each thread owns tile positions j*kNT + tid: their output rows.
     const uint32_t cnt = tr.row1 - tr.row0;
-    for (uint32_t j = threadIdx.x; j < cnt; j += kNT)
+    uint32_t dest[kRPT];
+#pragma unroll
+    for (int j = 0; j < kRPT; ++j)
     {
-        const uint32_t d = sorted_d[j];
-        out.keys[gbase[d] + (j - excl[d])] = stage64[j];
+        const uint32_t pos = j * kNT + threadIdx.x;
+        dest[j] = 0;
+        if (pos < cnt)
+        {
+            const uint32_t d = sorted_d[pos];
+            dest[j] = gbase[d] + (pos - excl[d]);
+            out.keys[dest[j]] = stage64[pos];
+        }
     }
     __syncthreads();
 
@@ -216,21 +214,11 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
     {
         switch (in.width[c])
         {
-            case 1:
-                scatter_column<uint8_t>((const uint8_t *)in.col[c], (uint8_t *)out.col[c], stage, sorted_d, excl, gbase, lp, tr);
-                break;
-            case 2:
-                scatter_column<uint16_t>((const uint16_t *)in.col[c], (uint16_t *)out.col[c], (uint16_t *)stage, sorted_d, excl, gbase, lp, tr);
-                break;
-            case 4:
-                scatter_column<uint32_t>((const uint32_t *)in.col[c], (uint32_t *)out.col[c], (uint32_t *)stage, sorted_d, excl, gbase, lp, tr);
-                break;
-            case 8:
-                scatter_column<uint64_t>((const uint64_t *)in.col[c], (uint64_t *)out.col[c], (uint64_t *)stage, sorted_d, excl, gbase, lp, tr);
-                break;
-            default:
-                scatter_column<uint4>((const uint4 *)in.col[c], (uint4 *)out.col[c], (uint4 *)stage, sorted_d, excl, gbase, lp, tr);
-                break;
+            case 1: scatter_column<uint8_t>((const uint8_t *)in.col[c], (uint8_t *)out.col[c], stage, lp, dest, tr); break;
+            case 2: scatter_column<uint16_t>((const uint16_t *)in.col[c], (uint16_t *)out.col[c], (uint16_t *)stage, lp, dest, tr); break;
+            case 4: scatter_column<uint32_t>((const uint32_t *)in.col[c], (uint32_t *)out.col[c], (uint32_t *)stage, lp, dest, tr); break;
+            case 8: scatter_column<uint64_t>((const uint64_t *)in.col[c], (uint64_t *)out.col[c], (uint64_t *)stage, lp, dest, tr); break;
+            default: scatter_column<uint4>((const uint4 *)in.col[c], (uint4 *)out.col[c], (uint4 *)stage, lp, dest, tr); break;
         }
     }
 }

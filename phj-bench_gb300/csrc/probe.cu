@@ -2,17 +2,19 @@
 // probeOneBlockCHJ, src/JoinOps.h:381-429; ProbeMaterialiser::gatherFromProbeBlock,
 // src/JoinOps.h:77-125).
 //
-// A persistent kernel streams the probe rows in chunks of 2048 taken from
-// a device work counter.  For each row it hashes the key, finds the leaf
-// (or CHJ sub-table) from the top hash bits, looks the key up (head
-// RowRefCell), and counts the matches by walking the next-chain when the
-// table holds duplicate keys.  A block-wide scan per 256-row round places
-// every match, one atomic per chunk reserves the chunk's output range, and
-// the rows are written column-major: key column (the probe key, as the
-// reference emits it), build payloads gathered through the RowRefCell, then
-// probe payloads.  This is the reference's "expand chains into flat
-// (probe_idx, build_ref) arrays, then gather" with the flat arrays kept in
-// registers instead of memory.
+// A persistent kernel walks the probe rows in chunks of 2048 (8 rounds of
+// 256 rows per CTA).  Per row: hash the key, locate the leaf table (or CHJ
+// sub-table) from the top hash bits, look the key up, and count the matches
+// (1, or the next-chain length when some build key repeats).  Each warp
+// scans its counts with shuffles; one shared-memory combine and one global
+// atomic per chunk place the chunk's output rows, warp-major and
+// round-major, so consecutive lanes write consecutive output rows.  The
+// projection then runs column by column -- key column (the probe key, as
+// the reference emits it), build payloads gathered through the RowRefCell,
+// probe payloads -- with each column's eight loads issued before its eight
+// stores.  This is the reference's "expand chains into flat
+// (probe_idx, build_ref) arrays, then gather column-major", with the flat
+// arrays held in registers.
 #include "internal.h"
 
 namespace phjg
@@ -21,7 +23,15 @@ namespace
 {
 constexpr int kPNT = 256;
 constexpr int kPRPT = 8;
+constexpr int kPWarps = kPNT / 32;
 constexpr uint32_t kChunk = kPNT * kPRPT;
+
+enum ProbeMode
+{
+    kLeafUniform = 0, // PHJ: every leaf table has 2^uniform_log2cap cells at leaf << log2cap
+    kLeafMeta = 1,    // PHJ: leaf tables located through the LeafMeta directory
+    kChj = 2          // CHJ: 256 sub-tables through LeafMeta; refs are (input block, row)
+};
 
 struct OutCols
 {
@@ -30,177 +40,267 @@ struct OutCols
     void * right[kMaxCols];
 };
 
-template <class T>
-__device__ __forceinline__ void put_stream(void * dst, uint64_t i, T v)
+// Build row (index into the build payload columns) of a RowRefCell.
+template <int kMode>
+__device__ __forceinline__ uint32_t build_row_of(uint64_t ref, const ProbeArgs & a)
 {
-    __stcs(static_cast<T *>(dst) + i, v);
-}
-
-__device__ __forceinline__ void copy_gather(void * dst, uint64_t di, const void * src, uint64_t si, uint32_t w)
-{
-    switch (w)
-    {
-        case 1: put_stream<uint8_t>(dst, di, __ldg(static_cast<const uint8_t *>(src) + si)); break;
-        case 2: put_stream<uint16_t>(dst, di, __ldg(static_cast<const uint16_t *>(src) + si)); break;
-        case 4: put_stream<uint32_t>(dst, di, __ldg(static_cast<const uint32_t *>(src) + si)); break;
-        case 8: put_stream<uint64_t>(dst, di, __ldg(static_cast<const uint64_t *>(src) + si)); break;
-        default: put_stream<uint4>(dst, di, __ldg(static_cast<const uint4 *>(src) + si)); break;
-    }
-}
-
-__device__ __forceinline__ void copy_stream(void * dst, uint64_t di, const void * src, uint64_t si, uint32_t w)
-{
-    switch (w)
-    {
-        case 1: put_stream<uint8_t>(dst, di, __ldcs(static_cast<const uint8_t *>(src) + si)); break;
-        case 2: put_stream<uint16_t>(dst, di, __ldcs(static_cast<const uint16_t *>(src) + si)); break;
-        case 4: put_stream<uint32_t>(dst, di, __ldcs(static_cast<const uint32_t *>(src) + si)); break;
-        case 8: put_stream<uint64_t>(dst, di, __ldcs(static_cast<const uint64_t *>(src) + si)); break;
-        default: put_stream<uint4>(dst, di, __ldcs(static_cast<const uint4 *>(src) + si)); break;
-    }
-}
-
-template <bool kCHJ>
-__device__ __forceinline__ uint64_t build_row_of(uint64_t ref, uint32_t leaf_row_off, const ProbeArgs & a)
-{
-    if (kCHJ)
+    if (kMode == kChj)
     {
         const uint32_t b = ref_block(ref);
         const uint64_t base = a.uniform_block_rows ? (uint64_t)b * a.uniform_block_rows : __ldg(a.block_off + b);
-        return base + ref_row(ref);
+        return (uint32_t)(base + ref_row(ref));
     }
-    return (uint64_t)leaf_row_off + ref_row(ref);
+    return ref_row(ref); // PHJ: {block 0 = the partitioned build rows, row}
 }
 
-template <bool kCHJ>
-__device__ __noinline__ uint32_t chain_length(uint64_t head, uint32_t roff, const ProbeArgs & a)
+__device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj)
 {
     uint32_t c = 1;
-    uint64_t r = __ldg(a.next + build_row_of<kCHJ>(head, roff, a));
+    uint64_t r = __ldg(a.next + brow);
     while (ref_valid(r))
     {
         ++c;
-        r = __ldg(a.next + build_row_of<kCHJ>(r, roff, a));
+        r = __ldg(a.next + (chj ? build_row_of<kChj>(r, a) : build_row_of<kLeafMeta>(r, a)));
     }
     return c;
 }
 
-// One output row: key column (probe key), build payloads via the
-// RowRefCell's row, probe payloads via the probe row.
-__device__ __forceinline__ void emit_row(const ProbeArgs & a, const OutCols & o, uint64_t brow, uint64_t key, uint64_t prow, uint64_t pos)
+template <class T>
+__device__ __forceinline__ void put(void * dst, uint64_t i, T v)
+{
+    __stcs(static_cast<T *>(dst) + i, v);
+}
+
+// One full output row (slow path for rows of duplicate-key chains).
+__device__ __forceinline__ void emit_row(const ProbeArgs & a, const OutCols & o, uint32_t brow, uint64_t key, uint64_t prow, uint64_t pos)
 {
     __stcs(o.keys + pos, key);
     for (uint32_t c = 0; c < a.build.n; ++c)
-        copy_gather(o.left[c], pos, a.build.col[c], brow, a.build.width[c]);
+        switch (a.build.width[c])
+        {
+            case 1: put<uint8_t>(o.left[c], pos, __ldg(static_cast<const uint8_t *>(a.build.col[c]) + brow)); break;
+            case 2: put<uint16_t>(o.left[c], pos, __ldg(static_cast<const uint16_t *>(a.build.col[c]) + brow)); break;
+            case 4: put<uint32_t>(o.left[c], pos, __ldg(static_cast<const uint32_t *>(a.build.col[c]) + brow)); break;
+            case 8: put<uint64_t>(o.left[c], pos, __ldg(static_cast<const uint64_t *>(a.build.col[c]) + brow)); break;
+            default: put<uint4>(o.left[c], pos, __ldg(static_cast<const uint4 *>(a.build.col[c]) + brow)); break;
+        }
     for (uint32_t c = 0; c < a.probe.n; ++c)
-        copy_stream(o.right[c], pos, a.probe.col[c], prow, a.probe.width[c]);
+        switch (a.probe.width[c])
+        {
+            case 1: put<uint8_t>(o.right[c], pos, static_cast<const uint8_t *>(a.probe.col[c])[prow]); break;
+            case 2: put<uint16_t>(o.right[c], pos, static_cast<const uint16_t *>(a.probe.col[c])[prow]); break;
+            case 4: put<uint32_t>(o.right[c], pos, static_cast<const uint32_t *>(a.probe.col[c])[prow]); break;
+            case 8: put<uint64_t>(o.right[c], pos, static_cast<const uint64_t *>(a.probe.col[c])[prow]); break;
+            default: put<uint4>(o.right[c], pos, static_cast<const uint4 *>(a.probe.col[c])[prow]); break;
+        }
 }
 
-template <bool kCHJ>
-__device__ __noinline__ void emit_chain(const ProbeArgs & a, const OutCols & o, uint64_t head, uint32_t roff, uint64_t key, uint64_t prow,
-                                        uint64_t pos, uint64_t out_cap)
+// Column pass over the chunk's match list: thread i writes output row
+// base + i, so every store of a column is coalesced; the loads are gathers
+// through the list (build rows) or nearly sequential (probe rows).
+template <class T, bool kBuild>
+__device__ __forceinline__ void column_pass(const void * src_v, void * dst_v, const uint32_t * idx, uint32_t n, uint64_t base)
 {
-    for (uint64_t r = head; ref_valid(r) && pos < out_cap; ++pos)
+    const T * src = static_cast<const T *>(src_v);
+    T * dst = static_cast<T *>(dst_v) + base;
+    uint32_t i = threadIdx.x;
+    for (; i + 3 * kPNT < n; i += 4 * kPNT)
     {
-        const uint64_t brow = build_row_of<kCHJ>(r, roff, a);
-        emit_row(a, o, brow, key, prow, pos);
-        r = __ldg(a.next + brow);
+        T v0, v1, v2, v3;
+        if (kBuild)
+        {
+            v0 = __ldg(src + idx[i]);
+            v1 = __ldg(src + idx[i + kPNT]);
+            v2 = __ldg(src + idx[i + 2 * kPNT]);
+            v3 = __ldg(src + idx[i + 3 * kPNT]);
+        }
+        else
+        {
+            v0 = __ldcs(src + idx[i]);
+            v1 = __ldcs(src + idx[i + kPNT]);
+            v2 = __ldcs(src + idx[i + 2 * kPNT]);
+            v3 = __ldcs(src + idx[i + 3 * kPNT]);
+        }
+        __stcs(dst + i, v0);
+        __stcs(dst + i + kPNT, v1);
+        __stcs(dst + i + 2 * kPNT, v2);
+        __stcs(dst + i + 3 * kPNT, v3);
     }
+    for (; i < n; i += kPNT)
+        __stcs(dst + i, kBuild ? __ldg(src + idx[i]) : __ldcs(src + idx[i]));
 }
 
-template <bool kCHJ>
-__global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o, unsigned long long * __restrict__ ctrs, uint64_t out_cap, int count_only)
+template <bool kBuild>
+__device__ __forceinline__ void columns_pass(const Cols & src, void * const * dst, const uint32_t * idx, uint32_t n, uint64_t base)
 {
-    // ctrs[0]: next chunk, ctrs[1]: output rows reserved
-    __shared__ uint32_t ws[kPNT / 32];
-    __shared__ uint32_t round_tot[kPRPT];
-    __shared__ unsigned long long sh_chunk, sh_base;
+#pragma unroll 1
+    for (uint32_t c = 0; c < src.n; ++c)
+        switch (src.width[c])
+        {
+            case 1: column_pass<uint8_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
+            case 2: column_pass<uint16_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
+            case 4: column_pass<uint32_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
+            case 8: column_pass<uint64_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
+            default: column_pass<uint4, kBuild>(src.col[c], dst[c], idx, n, base); break;
+        }
+}
+
+// Matches of one chunk, compacted in shared memory (the flat
+// (probe_idx, build_ref) arrays of probeOneBlock, plus the key).
+template <bool kDup>
+struct MatchList
+{
+    static constexpr uint32_t kCap = kDup ? 2 * kChunk : kChunk;
+    uint64_t key[kCap];
+    uint32_t brow[kCap];
+    uint32_t prow[kCap];
+};
+
+// kDup: some build key repeats, so rows may have several matches (chain
+// walks); without it every matched row yields exactly one output row and the
+// kernel carries no chain code at all.
+template <int kMode, bool kDup>
+__global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o,
+                                                unsigned long long * __restrict__ out_cursor, uint64_t out_cap, int count_only)
+{
+    extern __shared__ __align__(16) uint8_t smem_raw[];
+    MatchList<kDup> & ml = *reinterpret_cast<MatchList<kDup> *>(smem_raw);
+    __shared__ uint32_t warp_tot[kPWarps];
+    __shared__ uint32_t chunk_total;
+    __shared__ unsigned long long sh_base;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
     const uint32_t shift = 64u - a.leaf_bits;
-    for (;;)
+    const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
+    const uint64_t ucap = 1ull << ulog;
+    for (uint64_t chunk = blockIdx.x; chunk < n_chunks; chunk += gridDim.x)
     {
-        if (threadIdx.x == 0)
-            sh_chunk = atomicAdd(&ctrs[0], 1ull);
-        __syncthreads();
-        const uint64_t chunk = sh_chunk;
-        if (chunk >= n_chunks)
-            break;
-        const uint64_t row0 = chunk * kChunk;
-
-        uint64_t key[kPRPT], head[kPRPT];
-        uint32_t cnt[kPRPT], roff[kPRPT], excl[kPRPT];
-        uint8_t dupf[kPRPT];
+        const uint64_t row0 = chunk * kChunk + warp * 32 + lane; // + k * kPNT
+        uint64_t key[kPRPT];
+        uint32_t brow[kPRPT];
+        uint32_t valid = 0, dup = 0;
+        // ---- lookups: eight independent key -> table chains per thread
 #pragma unroll
         for (int k = 0; k < kPRPT; ++k)
         {
-            const uint64_t row = row0 + (uint64_t)k * kPNT + threadIdx.x;
-            head[k] = INVALID_REF;
+            const uint64_t row = row0 + (uint64_t)k * kPNT;
             key[k] = 0;
-            roff[k] = 0;
-            dupf[k] = 0;
+            brow[k] = 0;
             if (row < a.probe_rows)
             {
                 key[k] = __ldcs(a.probe.keys + row);
                 const uint64_t h = int_hash64(key[k]);
                 const uint32_t leaf = (uint32_t)(h >> shift);
-                const ulonglong2 mv = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + leaf));
-                const uint64_t table_off = mv.x;
-                const uint32_t row_off = (uint32_t)mv.y;
-                const uint32_t log2cap = (uint32_t)(mv.y >> 32) & 0xffu;
-                const uint32_t has = (uint32_t)(mv.y >> 40) & 0xffu;
-                dupf[k] = (uint8_t)((mv.y >> 48) & 0xffu);
-                roff[k] = row_off;
-                if (has)
-                    head[k] = table_find(a.cells + table_off, 1ull << log2cap, h, key[k]);
+                uint64_t head;
+                if (kMode == kLeafUniform)
+                {
+                    head = table_find(a.cells + ((uint64_t)leaf << ulog), ucap, h, key[k]);
+                    dup |= (kDup ? 1u : 0u) << k;
+                }
+                else
+                {
+                    const ulonglong2 mv = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + leaf));
+                    const uint32_t log2cap = (uint32_t)(mv.y >> 32) & 0xffu;
+                    const uint32_t has = (uint32_t)(mv.y >> 40) & 0xffu;
+                    if (kDup)
+                        dup |= (uint32_t)((mv.y >> 48) & 1u) << k;
+                    head = has ? table_find(a.cells + mv.x, 1ull << log2cap, h, key[k]) : INVALID_REF;
+                }
+                if (ref_valid(head))
+                {
+                    valid |= 1u << k;
+                    brow[k] = build_row_of<kMode>(head, a);
+                }
             }
         }
-#pragma unroll
-        for (int k = 0; k < kPRPT; ++k)
-            cnt[k] = !ref_valid(head[k]) ? 0u : (dupf[k] ? chain_length<kCHJ>(head[k], roff[k], a) : 1u);
+        dup &= valid;
+        // ---- counts and placement: warp scans, one combine per chunk
+        uint32_t excl[kPRPT];
+        uint32_t running = 0;
 #pragma unroll
         for (int k = 0; k < kPRPT; ++k)
         {
-            uint32_t tot;
-            excl[k] = block_excl_scan<kPNT>(cnt[k], ws, &tot);
-            if (threadIdx.x == 0)
-                round_tot[k] = tot;
+            uint32_t c = valid >> k & 1u;
+            if (kDup && (dup >> k & 1u))
+                c = chain_length(brow[k], a, kMode == kChj);
+            uint32_t x = c;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= (uint32_t)d)
+                    x += y;
+            }
+            excl[k] = running + x - c;
+            running += __shfl_sync(0xffffffffu, x, 31);
         }
+        if (lane == 0)
+            warp_tot[warp] = running;
+        __syncthreads();
         if (threadIdx.x == 0)
         {
-            uint64_t all = 0;
-            for (int k = 0; k < kPRPT; ++k)
-                all += round_tot[k];
-            sh_base = atomicAdd(&ctrs[1], (unsigned long long)all);
+            uint32_t acc = 0;
+            for (int w = 0; w < kPWarps; ++w)
+            {
+                const uint32_t t = warp_tot[w];
+                warp_tot[w] = acc;
+                acc += t;
+            }
+            chunk_total = acc;
+            sh_base = atomicAdd(out_cursor, (unsigned long long)acc);
         }
         __syncthreads();
+        if (count_only)
+            continue;
         const uint64_t base = sh_base;
-        uint64_t round_base = base;
-        if (!count_only)
-        {
+        const uint32_t total = chunk_total;
+        const uint32_t wbase = warp_tot[warp];
+        // ---- compact the matches into the chunk's list
 #pragma unroll
-            for (int k = 0; k < kPRPT; ++k)
+        for (int k = 0; k < kPRPT; ++k)
+        {
+            if (!(valid >> k & 1u))
+                continue;
+            uint32_t i = wbase + excl[k];
+            const uint32_t prow = (uint32_t)(row0 + (uint64_t)k * kPNT);
+            uint32_t b = brow[k];
+            for (;;)
             {
-                const uint64_t row = row0 + (uint64_t)k * kPNT + threadIdx.x;
-                if (ref_valid(head[k]))
+                if (i < MatchList<kDup>::kCap)
                 {
-                    const uint64_t pos = round_base + excl[k];
-                    if (dupf[k])
-                        emit_chain<kCHJ>(a, o, head[k], roff[k], key[k], row, pos, out_cap);
-                    else if (pos < out_cap)
-                        emit_row(a, o, build_row_of<kCHJ>(head[k], roff[k], a), key[k], row, pos);
+                    ml.key[i] = key[k];
+                    ml.brow[i] = b;
+                    ml.prow[i] = prow;
                 }
-                round_base += round_tot[k];
+                else if (base + i < out_cap) // past the list: written directly
+                    emit_row(a, o, b, key[k], prow, base + i);
+                if (!kDup || !(dup >> k & 1u))
+                    break;
+                const uint64_t r = __ldg(a.next + b);
+                if (!ref_valid(r))
+                    break;
+                b = build_row_of<kMode>(r, a);
+                ++i;
             }
         }
-        __syncthreads(); // round_tot / sh_chunk reuse
+        __syncthreads();
+        // ---- column passes: key, build payloads, probe payloads
+        uint32_t n = min(total, MatchList<kDup>::kCap);
+        if (base + n > out_cap)
+            n = base >= out_cap ? 0u : (uint32_t)(out_cap - base);
+        for (uint32_t i = threadIdx.x; i < n; i += kPNT)
+            __stcs(o.keys + base + i, ml.key[i]);
+        columns_pass<true>(a.build, o.left, ml.brow, n, base);
+        columns_pass<false>(a.probe, o.right, ml.prow, n, base);
+        __syncthreads(); // the list is rewritten by the next chunk
     }
 }
 } // namespace
 
 uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name)
 {
-    unsigned long long * ctrs = s.get<unsigned long long>(2);
-    PHJ_CUDA(cudaMemsetAsync(ctrs, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    unsigned long long * cursor = s.get<unsigned long long>(1);
+    PHJ_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), ctx->stream));
     OutCols o{};
     uint64_t cap = 0;
     if (out)
@@ -212,11 +312,13 @@ uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output 
             o.right[c] = out->rcol[c];
         cap = out->cap;
     }
+    const int mode = a.chj ? kChj : (a.uniform_log2cap >= 0 ? kLeafUniform : kLeafMeta);
+    auto kern = a.any_dup ? (mode == kChj ? k_probe<kChj, true> : mode == kLeafUniform ? k_probe<kLeafUniform, true> : k_probe<kLeafMeta, true>)
+                          : (mode == kChj ? k_probe<kChj, false> : mode == kLeafUniform ? k_probe<kLeafUniform, false> : k_probe<kLeafMeta, false>);
+    const size_t smem = a.any_dup ? sizeof(MatchList<true>) : sizeof(MatchList<false>);
+    PHJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    if (a.chj)
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe<true>, kPNT, 0));
-    else
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe<false>, kPNT, 0));
+    PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPNT, smem));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
     const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n_chunks, (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
     uint64_t probe_row_bytes = 8, build_row_bytes = 0;
@@ -226,17 +328,14 @@ uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output 
         build_row_bytes += a.build.width[c];
     {
         KTimer kt(ctx, name, a.probe_rows, count_only ? a.probe_rows * 8 : a.probe_rows * probe_row_bytes);
-        if (a.chj)
-            k_probe<true><<<grid, kPNT, 0, ctx->stream>>>(a, o, ctrs, cap, count_only ? 1 : 0);
-        else
-            k_probe<false><<<grid, kPNT, 0, ctx->stream>>>(a, o, ctrs, cap, count_only ? 1 : 0);
+        kern<<<grid, kPNT, smem, ctx->stream>>>(a, o, cursor, cap, count_only ? 1 : 0);
         PHJ_LAUNCHED(ctx, name);
     }
     unsigned long long rows = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&rows, ctrs + 1, sizeof(rows), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaMemcpyAsync(&rows, cursor, sizeof(rows), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    // Fix the algorithmic byte count of the timed launch now that the
-    // output size is known: output rows x (key + build + probe payloads).
+    // Algorithmic bytes of the timed launch, now that the output size is
+    // known: probe rows read + output rows (key + build + probe payloads).
     if (!count_only && !ctx->records.empty())
         ctx->records.back().bytes += rows * (8 + build_row_bytes + (probe_row_bytes - 8));
     return rows;
