@@ -388,6 +388,22 @@ phj_output * probe_into_output(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, 
 }
 } // namespace
 
+// A bounded device wait that gave up leaves a code in the error word; the
+// run fails with PHJ_ERR_DEVICE_TIMEOUT and the word is cleared.
+static void check_device_error(phj_ctx * ctx)
+{
+    int e = 0;
+    PHJ_CUDA(cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (e != 0)
+    {
+        PHJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), "a bounded device wait gave up (code %d)", e);
+        throw Error(PHJ_ERR_DEVICE_TIMEOUT, buf);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // schemes
 // ---------------------------------------------------------------------------
@@ -417,6 +433,7 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(e2));
+    check_device_error(ctx);
     if (res)
     {
         fill_phase(res->build, event_ms(e0, e1), B.rows);
@@ -482,6 +499,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(ev[4]));
+    check_device_error(ctx);
     if (res)
     {
         fill_phase(res->build_shuffle, event_ms(ev[0], ev[1]), B.rows);
@@ -542,6 +560,8 @@ phj_status phj_ctx_create(int device, phj_ctx ** out)
         PHJ_CUDA(cudaMemPoolCreate(&ctx->pool, &pp));
         uint64_t keep = ~0ull; // keep freed memory in the pool across runs
         PHJ_CUDA(cudaMemPoolSetAttribute(ctx->pool, cudaMemPoolAttrReleaseThreshold, &keep));
+        PHJ_CUDA(cudaMalloc(&ctx->d_err, sizeof(int)));
+        PHJ_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int)));
         set_partition_smem_limits((int)ctx->smem_optin);
         set_build_smem_limits((int)ctx->smem_optin);
     });
@@ -564,6 +584,8 @@ void phj_ctx_destroy(phj_ctx * ctx)
         cudaStreamSynchronize(ctx->stream);
     if (ctx->l2_flush)
         cudaFree(ctx->l2_flush);
+    if (ctx->d_err)
+        cudaFree(ctx->d_err);
     for (cudaEvent_t e : ctx->event_pool)
         cudaEventDestroy(e);
     for (auto & lv : ctx->live)

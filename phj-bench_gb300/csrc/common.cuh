@@ -205,3 +205,75 @@ __host__ __device__ __forceinline__ uint64_t bit_ceil64(uint64_t x)
 }
 
 } // namespace phjg
+
+// ---------------------------------------------------------------------------
+// Bulk asynchronous copies (cp.async.bulk, the TMA engine's 1-D form) into
+// shared memory, completed through an mbarrier.  Every wait is bounded: after
+// kWaitLimit polls it records `code` in the kernel's error word and gives up,
+// so a stuck copy surfaces as PHJ_ERR_DEVICE_TIMEOUT on the host instead of
+// a hung GPU.
+// ---------------------------------------------------------------------------
+namespace phjg
+{
+constexpr uint32_t kWaitLimit = 1u << 26;
+
+__device__ __forceinline__ uint32_t smem_u32(const void * p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t * bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes mbarrier initialisation visible to the async (bulk copy) proxy.
+__device__ __forceinline__ void fence_barrier_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Orders this thread's earlier generic-proxy shared-memory accesses before
+// later async-proxy ones (a bulk copy refilling a buffer threads just read).
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t * bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// Global -> shared bulk copy; dst, src 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_copy_g2s(void * dst, const void * src, uint32_t bytes, uint64_t * bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)), "l"(src),
+                 "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test_parity(uint64_t * bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Waits for phase `parity` of `bar` to complete; false (and *err = code) on
+// timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t * bar, uint32_t parity, int * err, int code)
+{
+    for (uint32_t i = 0; i < kWaitLimit; ++i)
+        if (mbar_test_parity(bar, parity))
+            return true;
+    atomicExch(err, code);
+    return false;
+}
+} // namespace phjg

@@ -83,6 +83,7 @@ struct phj_ctx
     size_t event_next = 0;
     void * l2_flush = nullptr;
     size_t l2_flush_bytes = 0;
+    int * d_err = nullptr; // device error word: bounded waits that gave up
     // Options (phj_ctx_set_int).
     int probe_materialize = -1; // -1 auto, 0 never, 1 always
 };

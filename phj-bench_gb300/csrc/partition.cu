@@ -223,6 +223,248 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
     }
 }
 
+// ---------------------------------------------------------------------------
+// First pass (one input segment): each CTA owns a contiguous range of whole
+// tiles, so the histogram is per CTA (digit-major, 2^b x G counts) and the
+// scatter keeps one running output cursor per digit in shared memory.  Tiles
+// arrive by bulk asynchronous copies (cp.async.bulk through the TMA engine)
+// into two shared-memory buffers: tile t+1 streams in while tile t is ranked
+// and written out, with no registers spent on prefetching.
+// ---------------------------------------------------------------------------
+constexpr int kP1NT = 512;
+
+struct P1Geom
+{
+    uint64_t n;
+    uint32_t tiles_per_cta;
+    uint32_t tile_rows;
+    uint32_t shift, b;
+};
+
+__global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__ keys, P1Geom g, uint32_t * __restrict__ counts)
+{
+    extern __shared__ uint32_t bins[];
+    const uint32_t nb = 1u << g.b, mask = nb - 1;
+    for (uint32_t i = threadIdx.x; i < nb; i += kP1NT)
+        bins[i] = 0;
+    __syncthreads();
+    const uint64_t r0 = (uint64_t)blockIdx.x * g.tiles_per_cta * g.tile_rows;
+    const uint64_t r1 = min(g.n, r0 + (uint64_t)g.tiles_per_cta * g.tile_rows);
+    for (uint64_t base = r0; base < r1; base += 8 * kP1NT)
+    {
+        uint64_t k[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const uint64_t row = base + j * kP1NT + threadIdx.x;
+            k[j] = row < r1 ? __ldcs(keys + row) : 0;
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+            if (base + j * kP1NT + threadIdx.x < r1)
+                atomicAdd(&bins[(uint32_t)(int_hash64(k[j]) >> g.shift) & mask], 1u);
+    }
+    __syncthreads();
+    for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+        counts[(uint64_t)d * gridDim.x + blockIdx.x] = bins[d];
+}
+
+struct P1Smem
+{
+    uint32_t buf_bytes;              // one tile of every column
+    uint32_t col_off[kMaxCols + 1];  // byte offset of each payload column in a buffer (keys at 0)
+};
+
+template <class T>
+__device__ __forceinline__ void p1_write_column(const uint8_t * buf, T * __restrict__ dst, const uint32_t (&src)[8], const uint32_t (&dest)[8], int rpt,
+                                                uint32_t cnt)
+{
+    const T * b = reinterpret_cast<const T *>(buf);
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+        if (j < rpt && j * kP1NT + threadIdx.x < cnt)
+            dst[dest[j]] = b[src[j]];
+}
+
+template <int RPT>
+__global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
+                                                         const __grid_constant__ P1Smem sm, const uint32_t * __restrict__ offs, int use_tma,
+                                                         int * __restrict__ err)
+{
+    constexpr uint32_t kT = kP1NT * RPT;
+    extern __shared__ __align__(16) uint8_t smem[];
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ uint32_t ws[kP1NT / 32];
+    uint8_t * buf[2] = {smem, smem + sm.buf_bytes};
+    uint16_t * inv = reinterpret_cast<uint16_t *>(smem + 2 * (size_t)sm.buf_bytes);
+    uint16_t * dsort = inv + kT;
+    const uint32_t nb = 1u << g.b, mask = nb - 1;
+    uint32_t * bins = reinterpret_cast<uint32_t *>(dsort + kT);
+    uint32_t * excl = bins + nb;
+    uint32_t * cursor = excl + nb;
+
+    const uint64_t n_tiles = ceil_div(g.n, kT);
+    const uint64_t t_begin = (uint64_t)blockIdx.x * g.tiles_per_cta;
+    const uint64_t t_end = min(n_tiles, t_begin + g.tiles_per_cta);
+    if (t_begin >= t_end)
+        return;
+    for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+        cursor[d] = offs[(uint64_t)d * gridDim.x + blockIdx.x];
+    if (threadIdx.x == 0)
+    {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    // A tile is fetched by bulk copy when every column slice is a whole
+    // number of 16-byte units (always, except a short last tile).
+    auto tile_rows = [&](uint64_t t) -> uint32_t { const uint64_t r = g.n - t * kT; return r < kT ? (uint32_t)r : kT; };
+    auto tma_ok = [&](uint64_t t) -> bool {
+        if (!use_tma)
+            return false;
+        const uint32_t r = tile_rows(t);
+        if ((r * 8u) & 15u)
+            return false;
+        for (uint32_t c = 0; c < in.n; ++c)
+            if ((r * in.width[c]) & 15u)
+                return false;
+        return true;
+    };
+    auto issue = [&](uint64_t t, int bi) {
+        const uint32_t r = tile_rows(t);
+        uint32_t bytes = r * 8u;
+        for (uint32_t c = 0; c < in.n; ++c)
+            bytes += r * in.width[c];
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bar[bi], bytes);
+        bulk_copy_g2s(buf[bi], in.keys + t * kT, r * 8u, &bar[bi]);
+        for (uint32_t c = 0; c < in.n; ++c)
+            bulk_copy_g2s(buf[bi] + sm.col_off[c], static_cast<const uint8_t *>(in.col[c]) + t * kT * in.width[c], r * in.width[c], &bar[bi]);
+    };
+    uint32_t parity[2] = {0, 0};
+    if (threadIdx.x == 0 && tma_ok(t_begin))
+        issue(t_begin, 0);
+
+    int bi = 0;
+    for (uint64_t t = t_begin; t < t_end; ++t, bi ^= 1)
+    {
+        const uint32_t cnt = tile_rows(t);
+        if (tma_ok(t))
+        {
+            const bool ok = mbar_wait(&bar[bi], parity[bi], err, 1);
+            if (!__syncthreads_and(ok))
+                break;
+            parity[bi] ^= 1u;
+        }
+        else
+        {
+            // plain cooperative loads of this tile
+            uint64_t * bk = reinterpret_cast<uint64_t *>(buf[bi]);
+            for (uint32_t i = threadIdx.x; i < cnt; i += kP1NT)
+                bk[i] = in.keys[t * kT + i];
+            for (uint32_t c = 0; c < in.n; ++c)
+                for (uint32_t i = threadIdx.x; i < cnt; i += kP1NT)
+                    copy_elem(buf[bi] + sm.col_off[c], i, in.col[c], t * kT + i, in.width[c]);
+        }
+        // prefetch the next tile into the other buffer (read last tile; the
+        // barrier at the end of the previous iteration ordered those reads)
+        if (threadIdx.x == 0 && t + 1 < t_end && tma_ok(t + 1))
+            issue(t + 1, bi ^ 1);
+        for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+            bins[d] = 0;
+        __syncthreads();
+
+        const uint64_t * bk = reinterpret_cast<const uint64_t *>(buf[bi]);
+        uint32_t dg[RPT], rk[RPT];
+#pragma unroll
+        for (int j = 0; j < RPT; ++j)
+        {
+            const uint32_t i = j * kP1NT + threadIdx.x;
+            dg[j] = 0xFFFFu;
+            rk[j] = 0;
+            if (i < cnt)
+            {
+                dg[j] = (uint32_t)(int_hash64(bk[i]) >> g.shift) & mask;
+                rk[j] = atomicAdd(&bins[dg[j]], 1u);
+            }
+        }
+        __syncthreads();
+        {
+            // exclusive scan of the tile's digit counts
+            const uint32_t per = (nb + kP1NT - 1) / kP1NT;
+            const uint32_t b0 = threadIdx.x * per;
+            uint32_t local = 0;
+            for (uint32_t i = 0; i < per; ++i)
+                if (b0 + i < nb)
+                    local += bins[b0 + i];
+            uint32_t total;
+            uint32_t run = block_excl_scan<kP1NT>(local, ws, &total);
+            for (uint32_t i = 0; i < per; ++i)
+                if (b0 + i < nb)
+                {
+                    excl[b0 + i] = run;
+                    run += bins[b0 + i];
+                }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < RPT; ++j)
+            if (dg[j] != 0xFFFFu)
+            {
+                const uint32_t pos = excl[dg[j]] + rk[j];
+                inv[pos] = (uint16_t)(j * kP1NT + threadIdx.x);
+                dsort[pos] = (uint16_t)dg[j];
+            }
+        __syncthreads();
+        uint32_t src[8], dest[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+        {
+            const uint32_t pos = j * kP1NT + threadIdx.x;
+            src[j] = 0;
+            dest[j] = 0;
+            if (j < RPT && pos < cnt)
+            {
+                const uint32_t d = dsort[pos];
+                src[j] = inv[pos];
+                dest[j] = cursor[d] + (pos - excl[d]);
+            }
+        }
+        p1_write_column<uint64_t>(buf[bi], out.keys, src, dest, RPT, cnt);
+        for (uint32_t c = 0; c < in.n; ++c)
+        {
+            const uint8_t * cb = buf[bi] + sm.col_off[c];
+            switch (in.width[c])
+            {
+                case 1: p1_write_column<uint8_t>(cb, (uint8_t *)out.col[c], src, dest, RPT, cnt); break;
+                case 2: p1_write_column<uint16_t>(cb, (uint16_t *)out.col[c], src, dest, RPT, cnt); break;
+                case 4: p1_write_column<uint32_t>(cb, (uint32_t *)out.col[c], src, dest, RPT, cnt); break;
+                case 8: p1_write_column<uint64_t>(cb, (uint64_t *)out.col[c], src, dest, RPT, cnt); break;
+                default: p1_write_column<uint4>(cb, (uint4 *)out.col[c], src, dest, RPT, cnt); break;
+            }
+        }
+        __syncthreads(); // cursor/bins reuse; this buffer may be refilled next iteration
+        for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+            cursor[d] += bins[d];
+    }
+    // A bulk copy still in flight (only after a timeout) must land before the
+    // CTA's shared memory is released.
+    if (threadIdx.x == 0 && *err)
+        for (int i = 0; i < 2; ++i)
+            (void)mbar_wait(&bar[i], parity[i], err, 1);
+}
+
+__global__ void k_p1_bucket_offsets(const uint32_t * __restrict__ offs, uint32_t nb, uint32_t G, uint32_t n, uint32_t * __restrict__ out_off)
+{
+    const uint32_t d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < nb)
+        out_off[d] = offs[(uint64_t)d * G];
+    else if (d == nb)
+        out_off[d] = n;
+}
+
 __global__ void k_tiles_per_seg(const uint32_t * __restrict__ seg_off, uint32_t n_segs, uint32_t * __restrict__ nt)
 {
     const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
@@ -256,6 +498,62 @@ __global__ void k_bucket_offsets(PassGeom g, const uint32_t * __restrict__ offs,
     out_off[i] = nt ? offs[(uint64_t)t0 * nb + (uint64_t)d * nt] : g.seg_off[s];
 }
 } // namespace
+
+// The first physical pass: histogram per CTA range, scan, bulk-copy fed
+// scatter with running cursors, then the bucket offsets.
+static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols & dst, uint64_t n, uint32_t b, uint32_t * bucket_off,
+                       const char * phase)
+{
+    const uint32_t nb = 1u << b;
+    uint64_t row_bytes = 8;
+    P1Smem sm{};
+    for (uint32_t c = 0; c < src.n; ++c)
+        row_bytes += src.width[c];
+    // rows per tile: the largest of 4096 / 2048 / 1024 whose two buffers fit
+    int rpt = 8;
+    size_t need = 0;
+    for (; rpt >= 2; rpt /= 2)
+    {
+        const uint64_t kT = (uint64_t)kP1NT * rpt;
+        need = 2 * kT * row_bytes + 4 * kT + 3ull * nb * 4 + 128;
+        if (need + 2048 <= ctx->smem_optin)
+            break;
+    }
+    if (rpt < 2)
+        throw Error(PHJ_ERR_UNSUPPORTED, "row too wide for the shared-memory tile of the partition pass");
+    const uint32_t kT = kP1NT * (uint32_t)rpt;
+    uint32_t off = kT * 8;
+    for (uint32_t c = 0; c < src.n; ++c)
+    {
+        sm.col_off[c] = off;
+        off += kT * src.width[c];
+    }
+    sm.buf_bytes = (off + 127) & ~127u;
+    need = 2ull * sm.buf_bytes + 4ull * kT + 3ull * nb * 4;
+    int per_sm = 1;
+    auto kern = rpt == 8 ? k_p1_scatter<8> : rpt == 4 ? k_p1_scatter<4> : k_p1_scatter<2>;
+    PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kP1NT, need));
+    const uint64_t n_tiles = ceil_div(n, kT);
+    const uint32_t G = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->num_sms * std::max(per_sm, 1)));
+    P1Geom g{n, (uint32_t)ceil_div(n_tiles, G), kT, 64u - b, b};
+    bool aligned = (reinterpret_cast<uintptr_t>(src.keys) & 15u) == 0;
+    for (uint32_t c = 0; c < src.n; ++c)
+        aligned = aligned && (reinterpret_cast<uintptr_t>(src.col[c]) & 15u) == 0;
+    uint32_t * counts = s.get<uint32_t>((uint64_t)nb * G + 1);
+    {
+        KTimer kt(ctx, "part_hist", n, n * 8);
+        k_p1_hist<<<G, kP1NT, nb * sizeof(uint32_t), ctx->stream>>>(src.keys, g, counts);
+        PHJ_LAUNCHED(ctx, "p1_hist");
+    }
+    scan_u32(ctx, s, counts, counts, (uint64_t)nb * G);
+    {
+        KTimer kt(ctx, phase, n, 2 * n * row_bytes);
+        kern<<<G, kP1NT, need, ctx->stream>>>(src, dst, g, sm, counts, aligned ? 1 : 0, ctx->d_err);
+        PHJ_LAUNCHED(ctx, "p1_scatter");
+    }
+    k_p1_bucket_offsets<<<(unsigned)ceil_div(nb + 1, 256), 256, 0, ctx->stream>>>(counts, nb, G, (uint32_t)n, bucket_off);
+    PHJ_LAUNCHED(ctx, "p1_offsets");
+}
 
 void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, const std::vector<uint32_t> & pass_bits, const Cols & out,
                      const Cols & tmp, uint32_t * leaf_off, const char * phase)
@@ -293,6 +591,17 @@ void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, co
         const uint32_t b = phys[p];
         const uint32_t nb = 1u << b;
         const Cols & dst = ((np - 1 - p) % 2 == 0) ? out : tmp;
+        if (n_segs == 1)
+        {
+            // first pass: contiguous tile ranges per CTA, bulk-copy fed
+            uint32_t * next_off = (p + 1 == np) ? leaf_off : s.get<uint32_t>((uint64_t)nb + 1);
+            first_pass(ctx, s, src, dst, n, b, next_off, phase);
+            seg_off = next_off;
+            n_segs = nb;
+            consumed += b;
+            src = dst;
+            continue;
+        }
         // Tiles of each segment, then their prefix.
         uint32_t * nt = s.get<uint32_t>(n_segs + 1);
         k_tiles_per_seg<<<(unsigned)ceil_div(n_segs, 256), 256, 0, ctx->stream>>>(seg_off, n_segs, nt);
@@ -333,6 +642,9 @@ void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, co
 
 void set_partition_smem_limits(int smem_optin)
 {
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
     // The scatter kernel stages a 4096-row tile of the widest column (<= 16
     // bytes) plus digit bins: up to ~96 KiB.
     const size_t need = (size_t)kTile * 16 + (size_t)kTile * sizeof(uint16_t) + 3ull * (1u << kMaxPassBits) * sizeof(uint32_t) + 128;
