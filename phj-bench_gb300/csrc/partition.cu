@@ -241,15 +241,24 @@ struct P1Geom
     uint32_t shift, b;
 };
 
-__global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__ keys, P1Geom g, uint32_t * __restrict__ counts)
+// H CTAs share one scatter CTA's row range (counts are zeroed first and
+// summed with global atomics), so the histogram keeps more loads in flight
+// than the scatter's one-CTA-per-SM grid would.
+__global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__ keys, P1Geom g, uint32_t H, uint32_t G,
+                                                   uint32_t * __restrict__ counts)
 {
     extern __shared__ uint32_t bins[];
     const uint32_t nb = 1u << g.b, mask = nb - 1;
     for (uint32_t i = threadIdx.x; i < nb; i += kP1NT)
         bins[i] = 0;
     __syncthreads();
-    const uint64_t r0 = (uint64_t)blockIdx.x * g.tiles_per_cta * g.tile_rows;
-    const uint64_t r1 = min(g.n, r0 + (uint64_t)g.tiles_per_cta * g.tile_rows);
+    const uint32_t gi = blockIdx.x / H, q = blockIdx.x % H;
+    const uint64_t span = (uint64_t)g.tiles_per_cta * g.tile_rows;
+    const uint64_t g0 = (uint64_t)gi * span;
+    const uint64_t g1 = min(g.n, g0 + span);
+    const uint64_t part = ceil_div(span, (uint64_t)H * 8 * kP1NT) * 8 * kP1NT;
+    const uint64_t r0 = g0 + q * part;
+    const uint64_t r1 = min(g1, r0 + part);
     for (uint64_t base = r0; base < r1; base += 8 * kP1NT)
     {
         uint64_t k[8];
@@ -266,7 +275,8 @@ __global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__
     }
     __syncthreads();
     for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
-        counts[(uint64_t)d * gridDim.x + blockIdx.x] = bins[d];
+        if (bins[d])
+            atomicAdd(&counts[(uint64_t)d * G + gi], bins[d]);
 }
 
 struct P1Smem
@@ -275,28 +285,28 @@ struct P1Smem
     uint32_t col_off[kMaxCols + 1];  // byte offset of each payload column in a buffer (keys at 0)
 };
 
-template <class T>
-__device__ __forceinline__ void p1_write_column(const uint8_t * buf, T * __restrict__ dst, const uint32_t (&src)[8], const uint32_t (&dest)[8], int rpt,
+template <class T, int RPT>
+__device__ __forceinline__ void p1_write_column(const uint8_t * buf, T * __restrict__ dst, const uint32_t (&src)[RPT], const uint32_t (&dest)[RPT],
                                                 uint32_t cnt)
 {
     const T * b = reinterpret_cast<const T *>(buf);
 #pragma unroll
-    for (int j = 0; j < 8; ++j)
-        if (j < rpt && j * kP1NT + threadIdx.x < cnt)
+    for (int j = 0; j < RPT; ++j)
+        if (j * kP1NT + threadIdx.x < cnt)
             dst[dest[j]] = b[src[j]];
 }
 
 template <int RPT>
 __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
-                                                         const __grid_constant__ P1Smem sm, const uint32_t * __restrict__ offs, int use_tma,
-                                                         int * __restrict__ err)
+                                                         const __grid_constant__ P1Smem sm, uint32_t stages, const uint32_t * __restrict__ offs,
+                                                         int use_tma, int * __restrict__ err)
 {
     constexpr uint32_t kT = kP1NT * RPT;
+    constexpr uint32_t kMaxStages = 4;
     extern __shared__ __align__(16) uint8_t smem[];
-    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ __align__(8) uint64_t bar[kMaxStages];
     __shared__ uint32_t ws[kP1NT / 32];
-    uint8_t * buf[2] = {smem, smem + sm.buf_bytes};
-    uint16_t * inv = reinterpret_cast<uint16_t *>(smem + 2 * (size_t)sm.buf_bytes);
+    uint16_t * inv = reinterpret_cast<uint16_t *>(smem + (size_t)stages * sm.buf_bytes);
     uint16_t * dsort = inv + kT;
     const uint32_t nb = 1u << g.b, mask = nb - 1;
     uint32_t * bins = reinterpret_cast<uint32_t *>(dsort + kT);
@@ -312,8 +322,8 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
         cursor[d] = offs[(uint64_t)d * gridDim.x + blockIdx.x];
     if (threadIdx.x == 0)
     {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (uint32_t i = 0; i < stages; ++i)
+            mbar_init(&bar[i], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -332,51 +342,55 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
                 return false;
         return true;
     };
-    auto issue = [&](uint64_t t, int bi) {
+    auto buffer = [&](uint32_t i) -> uint8_t * { return smem + (size_t)i * sm.buf_bytes; };
+    auto issue = [&](uint64_t t, uint32_t bi) {
         const uint32_t r = tile_rows(t);
         uint32_t bytes = r * 8u;
         for (uint32_t c = 0; c < in.n; ++c)
             bytes += r * in.width[c];
         fence_proxy_async_smem();
         mbar_arrive_expect_tx(&bar[bi], bytes);
-        bulk_copy_g2s(buf[bi], in.keys + t * kT, r * 8u, &bar[bi]);
+        bulk_copy_g2s(buffer(bi), in.keys + t * kT, r * 8u, &bar[bi]);
         for (uint32_t c = 0; c < in.n; ++c)
-            bulk_copy_g2s(buf[bi] + sm.col_off[c], static_cast<const uint8_t *>(in.col[c]) + t * kT * in.width[c], r * in.width[c], &bar[bi]);
+            bulk_copy_g2s(buffer(bi) + sm.col_off[c], static_cast<const uint8_t *>(in.col[c]) + t * kT * in.width[c], r * in.width[c], &bar[bi]);
     };
-    uint32_t parity[2] = {0, 0};
-    if (threadIdx.x == 0 && tma_ok(t_begin))
-        issue(t_begin, 0);
+    uint32_t parity = 0; // bit i: phase of bar[i] to wait for
+    if (threadIdx.x == 0)
+        for (uint32_t i = 0; i + 1 < stages && t_begin + i < t_end; ++i)
+            if (tma_ok(t_begin + i))
+                issue(t_begin + i, i);
 
-    int bi = 0;
-    for (uint64_t t = t_begin; t < t_end; ++t, bi ^= 1)
+    uint32_t bi = 0;
+    for (uint64_t t = t_begin; t < t_end; ++t, bi = (bi + 1 == stages) ? 0 : bi + 1)
     {
         const uint32_t cnt = tile_rows(t);
+        uint8_t * buf = buffer(bi);
         if (tma_ok(t))
         {
-            const bool ok = mbar_wait(&bar[bi], parity[bi], err, 1);
+            const bool ok = mbar_wait(&bar[bi], (parity >> bi) & 1u, err, 1);
             if (!__syncthreads_and(ok))
                 break;
-            parity[bi] ^= 1u;
+            parity ^= 1u << bi;
         }
         else
         {
-            // plain cooperative loads of this tile
-            uint64_t * bk = reinterpret_cast<uint64_t *>(buf[bi]);
+            uint64_t * bk = reinterpret_cast<uint64_t *>(buf);
             for (uint32_t i = threadIdx.x; i < cnt; i += kP1NT)
                 bk[i] = in.keys[t * kT + i];
             for (uint32_t c = 0; c < in.n; ++c)
                 for (uint32_t i = threadIdx.x; i < cnt; i += kP1NT)
-                    copy_elem(buf[bi] + sm.col_off[c], i, in.col[c], t * kT + i, in.width[c]);
+                    copy_elem(buf + sm.col_off[c], i, in.col[c], t * kT + i, in.width[c]);
         }
-        // prefetch the next tile into the other buffer (read last tile; the
-        // barrier at the end of the previous iteration ordered those reads)
-        if (threadIdx.x == 0 && t + 1 < t_end && tma_ok(t + 1))
-            issue(t + 1, bi ^ 1);
+        // keep stages-1 tiles in flight: refill the buffer the previous tile
+        // used (its readers finished at the barrier ending that iteration)
+        const uint32_t nbi = (bi + stages - 1) % stages;
+        if (threadIdx.x == 0 && t + stages - 1 < t_end && tma_ok(t + stages - 1))
+            issue(t + stages - 1, nbi);
         for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
             bins[d] = 0;
         __syncthreads();
 
-        const uint64_t * bk = reinterpret_cast<const uint64_t *>(buf[bi]);
+        const uint64_t * bk = reinterpret_cast<const uint64_t *>(buf);
         uint32_t dg[RPT], rk[RPT];
 #pragma unroll
         for (int j = 0; j < RPT; ++j)
@@ -392,7 +406,6 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
         }
         __syncthreads();
         {
-            // exclusive scan of the tile's digit counts
             const uint32_t per = (nb + kP1NT - 1) / kP1NT;
             const uint32_t b0 = threadIdx.x * per;
             uint32_t local = 0;
@@ -418,42 +431,42 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
                 dsort[pos] = (uint16_t)dg[j];
             }
         __syncthreads();
-        uint32_t src[8], dest[8];
+        uint32_t src[RPT], dest[RPT];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < RPT; ++j)
         {
             const uint32_t pos = j * kP1NT + threadIdx.x;
             src[j] = 0;
             dest[j] = 0;
-            if (j < RPT && pos < cnt)
+            if (pos < cnt)
             {
                 const uint32_t d = dsort[pos];
                 src[j] = inv[pos];
                 dest[j] = cursor[d] + (pos - excl[d]);
             }
         }
-        p1_write_column<uint64_t>(buf[bi], out.keys, src, dest, RPT, cnt);
+        p1_write_column<uint64_t, RPT>(buf, out.keys, src, dest, cnt);
         for (uint32_t c = 0; c < in.n; ++c)
         {
-            const uint8_t * cb = buf[bi] + sm.col_off[c];
+            const uint8_t * cb = buf + sm.col_off[c];
             switch (in.width[c])
             {
-                case 1: p1_write_column<uint8_t>(cb, (uint8_t *)out.col[c], src, dest, RPT, cnt); break;
-                case 2: p1_write_column<uint16_t>(cb, (uint16_t *)out.col[c], src, dest, RPT, cnt); break;
-                case 4: p1_write_column<uint32_t>(cb, (uint32_t *)out.col[c], src, dest, RPT, cnt); break;
-                case 8: p1_write_column<uint64_t>(cb, (uint64_t *)out.col[c], src, dest, RPT, cnt); break;
-                default: p1_write_column<uint4>(cb, (uint4 *)out.col[c], src, dest, RPT, cnt); break;
+                case 1: p1_write_column<uint8_t, RPT>(cb, (uint8_t *)out.col[c], src, dest, cnt); break;
+                case 2: p1_write_column<uint16_t, RPT>(cb, (uint16_t *)out.col[c], src, dest, cnt); break;
+                case 4: p1_write_column<uint32_t, RPT>(cb, (uint32_t *)out.col[c], src, dest, cnt); break;
+                case 8: p1_write_column<uint64_t, RPT>(cb, (uint64_t *)out.col[c], src, dest, cnt); break;
+                default: p1_write_column<uint4, RPT>(cb, (uint4 *)out.col[c], src, dest, cnt); break;
             }
         }
-        __syncthreads(); // cursor/bins reuse; this buffer may be refilled next iteration
+        __syncthreads(); // cursor/bins reuse; this buffer is refilled next iteration
         for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
             cursor[d] += bins[d];
     }
-    // A bulk copy still in flight (only after a timeout) must land before the
-    // CTA's shared memory is released.
+    // Bulk copies still in flight (only after a timeout) must land before
+    // the CTA's shared memory is released.
     if (threadIdx.x == 0 && *err)
-        for (int i = 0; i < 2; ++i)
-            (void)mbar_wait(&bar[i], parity[i], err, 1);
+        for (uint32_t i = 0; i < stages; ++i)
+            (void)mbar_wait(&bar[i], (parity >> i) & 1u, err, 1);
 }
 
 __global__ void k_p1_bucket_offsets(const uint32_t * __restrict__ offs, uint32_t nb, uint32_t G, uint32_t n, uint32_t * __restrict__ out_off)
@@ -509,17 +522,31 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
     P1Smem sm{};
     for (uint32_t c = 0; c < src.n; ++c)
         row_bytes += src.width[c];
-    // rows per tile: the largest of 4096 / 2048 / 1024 whose two buffers fit
-    int rpt = 8;
-    size_t need = 0;
-    for (; rpt >= 2; rpt /= 2)
-    {
-        const uint64_t kT = (uint64_t)kP1NT * rpt;
-        need = 2 * kT * row_bytes + 4 * kT + 3ull * nb * 4 + 128;
-        if (need + 2048 <= ctx->smem_optin)
-            break;
-    }
-    if (rpt < 2)
+    // Tile rows (4096/2048/1024) and ring depth (2-4): the pair that keeps
+    // the most bytes in flight ((stages - 1) tiles) within shared memory.
+    int rpt = 0;
+    uint32_t stages = 0;
+    uint64_t best = 0;
+    for (int r = 8; r >= 2; r /= 2)
+        for (uint32_t st = 2; st <= 4; ++st)
+        {
+            const uint64_t kT = (uint64_t)kP1NT * r;
+            uint64_t buf = kT * 8;
+            for (uint32_t c = 0; c < src.n; ++c)
+                buf += kT * src.width[c];
+            buf = (buf + 127) & ~127ull;
+            const uint64_t need_rs = st * buf + 4 * kT + 3ull * nb * 4;
+            if (need_rs + 2048 > ctx->smem_optin)
+                continue;
+            const uint64_t inflight = (st - 1) * buf;
+            if (inflight > best)
+            {
+                best = inflight;
+                rpt = r;
+                stages = st;
+            }
+        }
+    if (rpt == 0)
         throw Error(PHJ_ERR_UNSUPPORTED, "row too wide for the shared-memory tile of the partition pass");
     const uint32_t kT = kP1NT * (uint32_t)rpt;
     uint32_t off = kT * 8;
@@ -529,7 +556,7 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
         off += kT * src.width[c];
     }
     sm.buf_bytes = (off + 127) & ~127u;
-    need = 2ull * sm.buf_bytes + 4ull * kT + 3ull * nb * 4;
+    const size_t need = (size_t)stages * sm.buf_bytes + 4ull * kT + 3ull * nb * 4;
     int per_sm = 1;
     auto kern = rpt == 8 ? k_p1_scatter<8> : rpt == 4 ? k_p1_scatter<4> : k_p1_scatter<2>;
     PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kP1NT, need));
@@ -540,15 +567,17 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
     for (uint32_t c = 0; c < src.n; ++c)
         aligned = aligned && (reinterpret_cast<uintptr_t>(src.col[c]) & 15u) == 0;
     uint32_t * counts = s.get<uint32_t>((uint64_t)nb * G + 1);
+    PHJ_CUDA(cudaMemsetAsync(counts, 0, ((uint64_t)nb * G + 1) * sizeof(uint32_t), ctx->stream));
     {
+        const uint32_t H = 4;
         KTimer kt(ctx, "part_hist", n, n * 8);
-        k_p1_hist<<<G, kP1NT, nb * sizeof(uint32_t), ctx->stream>>>(src.keys, g, counts);
+        k_p1_hist<<<G * H, kP1NT, nb * sizeof(uint32_t), ctx->stream>>>(src.keys, g, H, G, counts);
         PHJ_LAUNCHED(ctx, "p1_hist");
     }
     scan_u32(ctx, s, counts, counts, (uint64_t)nb * G);
     {
         KTimer kt(ctx, phase, n, 2 * n * row_bytes);
-        kern<<<G, kP1NT, need, ctx->stream>>>(src, dst, g, sm, counts, aligned ? 1 : 0, ctx->d_err);
+        kern<<<G, kP1NT, need, ctx->stream>>>(src, dst, g, sm, stages, counts, aligned ? 1 : 0, ctx->d_err);
         PHJ_LAUNCHED(ctx, "p1_scatter");
     }
     k_p1_bucket_offsets<<<(unsigned)ceil_div(nb + 1, 256), 256, 0, ctx->stream>>>(counts, nb, G, (uint32_t)n, bucket_off);

@@ -159,9 +159,54 @@ struct MatchList
 // kDup: some build key repeats, so rows may have several matches (chain
 // walks); without it every matched row yields exactly one output row and the
 // kernel carries no chain code at all.
+// Chunk status words for the decoupled look-back that places each chunk's
+// output rows: flag in the top two bits, row count below.
+constexpr unsigned long long kFlagAgg = 1ull << 62;  // the chunk's own total
+constexpr unsigned long long kFlagIncl = 2ull << 62; // total of chunks 0..c
+constexpr unsigned long long kValMask = (1ull << 62) - 1;
+
+// Publishes chunk c's total and finds the rows of all earlier chunks.  Only
+// thread 0 of the CTA calls it.  Chunks are taken in increasing order by
+// co-resident CTAs (cooperative launch), so the lowest unfinished chunk
+// never waits; every wait is still bounded.
+__device__ __forceinline__ unsigned long long chunk_base(unsigned long long * status, uint64_t c, uint32_t total, int * err)
+{
+    if (c == 0)
+    {
+        atomicExch(status, kFlagIncl | total);
+        return 0;
+    }
+    atomicExch(status + c, kFlagAgg | total);
+    unsigned long long acc = 0;
+    uint64_t j = c - 1;
+    for (uint32_t spins = 0;;)
+    {
+        const unsigned long long st = *reinterpret_cast<volatile unsigned long long *>(status + j);
+        if (st & kFlagIncl)
+        {
+            acc += st & kValMask;
+            break;
+        }
+        if (st & kFlagAgg)
+        {
+            acc += st & kValMask;
+            --j; // chunk 0 always holds an inclusive value
+            continue;
+        }
+        if (++spins >= kWaitLimit)
+        {
+            atomicExch(err, 2);
+            return ~0ull;
+        }
+    }
+    atomicExch(status + c, kFlagIncl | (acc + total));
+    return acc;
+}
+
 template <int kMode, bool kDup>
 __global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o,
-                                                unsigned long long * __restrict__ out_cursor, uint64_t out_cap, int count_only)
+                                                unsigned long long * __restrict__ status, uint64_t out_cap, int count_only,
+                                                int * __restrict__ err)
 {
     extern __shared__ __align__(16) uint8_t smem_raw[];
     MatchList<kDup> & ml = *reinterpret_cast<MatchList<kDup> *>(smem_raw);
@@ -247,10 +292,10 @@ __global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArg
                 acc += t;
             }
             chunk_total = acc;
-            sh_base = atomicAdd(out_cursor, (unsigned long long)acc);
+            sh_base = chunk_base(status, chunk, acc, err);
         }
         __syncthreads();
-        if (count_only)
+        if (count_only || sh_base == ~0ull)
             continue;
         const uint64_t base = sh_base;
         const uint32_t total = chunk_total;
@@ -299,8 +344,9 @@ __global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArg
 
 uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name)
 {
-    unsigned long long * cursor = s.get<unsigned long long>(1);
-    PHJ_CUDA(cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), ctx->stream));
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
+    unsigned long long * status = s.get<unsigned long long>(n_chunks + 1);
+    PHJ_CUDA(cudaMemsetAsync(status, 0, (n_chunks + 1) * sizeof(unsigned long long), ctx->stream));
     OutCols o{};
     uint64_t cap = 0;
     if (out)
@@ -319,8 +365,9 @@ uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output 
     PHJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
     PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPNT, smem));
-    const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
-    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n_chunks, (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
+    // Every CTA must be resident (the look-back waits on other CTAs'
+    // chunks): a cooperative launch of at most one wave.
+    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(std::max<uint64_t>(n_chunks, 1), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
     uint64_t probe_row_bytes = 8, build_row_bytes = 0;
     for (uint32_t c = 0; c < a.probe.n; ++c)
         probe_row_bytes += a.probe.width[c];
@@ -328,12 +375,17 @@ uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output 
         build_row_bytes += a.build.width[c];
     {
         KTimer kt(ctx, name, a.probe_rows, count_only ? a.probe_rows * 8 : a.probe_rows * probe_row_bytes);
-        kern<<<grid, kPNT, smem, ctx->stream>>>(a, o, cursor, cap, count_only ? 1 : 0);
+        int co = count_only ? 1 : 0;
+        ProbeArgs aa = a;
+        void * args[] = {&aa, &o, &status, &cap, &co, &ctx->d_err};
+        PHJ_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kPNT), args, smem, ctx->stream));
         PHJ_LAUNCHED(ctx, name);
     }
-    unsigned long long rows = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&rows, cursor, sizeof(rows), cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long last = 0;
+    if (n_chunks)
+        PHJ_CUDA(cudaMemcpyAsync(&last, status + n_chunks - 1, sizeof(last), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    const uint64_t rows = last & kValMask;
     // Algorithmic bytes of the timed launch, now that the output size is
     // known: probe rows read + output rows (key + build + probe payloads).
     if (!count_only && !ctx->records.empty())
