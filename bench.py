@@ -260,6 +260,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-chj", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="multiply both sides' rows (profiling on a smaller case)")
+    ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="context option (phj_ctx_set_int)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = Dist(world)
@@ -274,6 +275,9 @@ def main():
         scale_workload(args.workload, args.scale)
         desc, _, bspec, pspec, _ = WORKLOADS[args.workload]
     ctx = P.Context(local)
+    for kv in args.set:
+        k, v = kv.split("=")
+        ctx.set_int(k, int(v))
     b, p = make_tables(ctx, args.workload)
     B, Pn = b.rows, p.rows
     tuples = B + Pn
@@ -331,7 +335,7 @@ def main():
         "dtype": "u64", "data": "synthetic (seeded device generator; keys, payloads and match rate as specified)",
         "config": {"workload": desc, "scheme": scheme, "build_rows": B, "probe_rows": Pn, "radix_pass_bits": bits,
                    "output_rows": out_rows, "l2": "inputs larger than L2 (probe side 4.3 GB) and an L2 flush between steps",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload),
                      "bytes_per_launch": bytes_per_launch, "ms_per_launch": avg_ms, "peak_source": peak_src},

@@ -226,6 +226,8 @@ void check_sides(const phj_table * b, const phj_table * p)
         throw Error(PHJ_ERR_UNSUPPORTED, "device schemes support < 2^31 build rows and < 2^32 probe rows");
 }
 
+} // namespace
+
 phj_output * new_output(phj_ctx * ctx, const phj_schema & left, const phj_schema & right, uint64_t cap)
 {
     phj_output * o = new phj_output();
@@ -273,6 +275,9 @@ void free_output(phj_ctx * ctx, phj_output * o)
     }
     delete o;
 }
+
+namespace
+{
 
 void set_block_structure(phj_ctx * ctx, phj_table * t, uint32_t n_blocks, const uint32_t * block_rows)
 {
@@ -365,26 +370,9 @@ Cols payload_cols(const Cols & c)
     return p;
 }
 
-// Sizes the output: probe rows bound the output when no build key repeats;
-// otherwise a count-only probe gives the exact size first.
 phj_output * probe_into_output(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
 {
-    uint64_t cap = a.probe_rows;
-    if (a.any_dup)
-        cap = probe_join(ctx, s, a, nullptr, true, "probe_count");
-    phj_output * out = new_output(ctx, left, right, cap);
-    try
-    {
-        out->rows = probe_join(ctx, s, a, out, false, "probe_join");
-        if (out->rows > out->cap)
-            throw Error(PHJ_ERR_CAPACITY, "probe produced more rows than its counted capacity");
-    }
-    catch (...)
-    {
-        free_output(ctx, out);
-        throw;
-    }
-    return out;
+    return probe_join(ctx, s, a, left, right);
 }
 } // namespace
 

@@ -253,6 +253,13 @@ __device__ __forceinline__ void bulk_copy_g2s(void * dst, const void * src, uint
                  : "memory");
 }
 
+// Bulk prefetch of [src, src + bytes) into L2 by the TMA engine (no
+// registers, no shared memory); src 16-byte aligned, bytes % 16 == 0.
+__device__ __forceinline__ void bulk_prefetch_l2(const void * src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 __device__ __forceinline__ bool mbar_test_parity(uint64_t * bar, uint32_t parity)
 {
     uint32_t ok;

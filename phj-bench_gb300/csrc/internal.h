@@ -225,8 +225,10 @@ struct ProbeArgs
     int any_dup;
     int uniform_log2cap;    // >= 0: PHJ leaf tables of uniform capacity (no directory lookup)
 };
-// Returns the number of output rows; writes them to `out` unless count_only.
-uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name);
+// Lookups, then an exactly sized output, then the projection.
+phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);
+phj_output * new_output(phj_ctx * ctx, const phj_schema & left, const phj_schema & right, uint64_t cap);
+void free_output(phj_ctx * ctx, phj_output * o);
 
 // ----- gen.cu -----------------------------------------------------------------------------
 // Fills t's columns; returns the number of distinct build keys for kinds 0/2.

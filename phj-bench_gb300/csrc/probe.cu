@@ -2,20 +2,27 @@
 // probeOneBlockCHJ, src/JoinOps.h:381-429; ProbeMaterialiser::gatherFromProbeBlock,
 // src/JoinOps.h:77-125).
 //
-// A persistent kernel walks the probe rows in chunks of 2048 (8 rounds of
-// 256 rows per CTA).  Per row: hash the key, locate the leaf table (or CHJ
-// sub-table) from the top hash bits, look the key up, and count the matches
-// (1, or the next-chain length when some build key repeats).  Each warp
-// scans its counts with shuffles; one shared-memory combine and one global
-// atomic per chunk place the chunk's output rows, warp-major and
-// round-major, so consecutive lanes write consecutive output rows.  The
-// projection then runs column by column -- key column (the probe key, as
-// the reference emits it), build payloads gathered through the RowRefCell,
-// probe payloads -- with each column's eight loads issued before its eight
-// stores.  This is the reference's "expand chains into flat
-// (probe_idx, build_ref) arrays, then gather column-major", with the flat
-// arrays held in registers.
+// Two barrier-free kernels whose warps are independent workers over chunks
+// of 256 probe rows, taken in increasing order across the grid so the whole
+// grid sweeps the probe side front to back and the leaf tables of the rows
+// in flight stay in L2:
+//   k_probe_lookup   hash each key, locate its leaf table (or CHJ sub-table)
+//                    from the top hash bits, look it up, and record the head
+//                    build row (or none) per probe row plus the chunk's
+//                    match count (1 per hit, or the next-chain length when
+//                    some build key repeats);
+//   scan_u32         chunk counts -> each chunk's first output row;
+//   k_probe_project  re-walk the chunk, place each match with a warp scan,
+//                    and write the output column-major: key column (the
+//                    probe key, as the reference emits it), build payloads
+//                    gathered through the RowRefCell, probe payloads.
+// This is the reference's "batchFind heads, expand chains into flat
+// (probe_idx, build_ref) arrays, then gather column-major" with the head
+// array in memory and the expansion folded into the projection.
 #include "internal.h"
+
+#include <cstdio>
+#include <cstdlib>
 
 namespace phjg
 {
@@ -24,7 +31,8 @@ namespace
 constexpr int kPNT = 256;
 constexpr int kPRPT = 8;
 constexpr int kPWarps = kPNT / 32;
-constexpr uint32_t kChunk = kPNT * kPRPT;
+constexpr uint32_t kWChunk = 32 * kPRPT; // probe rows per warp chunk
+constexpr uint32_t kNoMatch = 0xFFFFFFFFu;
 
 enum ProbeMode
 {
@@ -40,6 +48,19 @@ struct OutCols
     void * right[kMaxCols];
 };
 
+// Every output column as one list for the projection loop: the key column
+// (from the probe keys), the build payloads (gathered by build row), the
+// probe payloads (by probe row).
+constexpr int kMaxOutCols = 1 + 2 * kMaxCols;
+struct ProjCols
+{
+    const void * src[kMaxOutCols];
+    void * dst[kMaxOutCols];
+    uint8_t width[kMaxOutCols];
+    uint8_t by_build[kMaxOutCols];
+    uint32_t n;
+};
+
 // Build row (index into the build payload columns) of a RowRefCell.
 template <int kMode>
 __device__ __forceinline__ uint32_t build_row_of(uint64_t ref, const ProbeArgs & a)
@@ -51,6 +72,23 @@ __device__ __forceinline__ uint32_t build_row_of(uint64_t ref, const ProbeArgs &
         return (uint32_t)(base + ref_row(ref));
     }
     return ref_row(ref); // PHJ: {block 0 = the partitioned build rows, row}
+}
+
+// Linear probing from cell `pos` on (the first cell collided).
+__device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t cap, uint64_t pos, uint64_t key)
+{
+    const uint64_t mask = cap - 1;
+    pos &= mask;
+    for (uint64_t step = 1; step < cap; ++step)
+    {
+        const ulonglong2 c = __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
+        if (!ref_valid(c.y))
+            return INVALID_REF;
+        if (c.x == key)
+            return c.y;
+        pos = (pos + 1) & mask;
+    }
+    return INVALID_REF;
 }
 
 __device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj)
@@ -95,302 +133,378 @@ __device__ __forceinline__ void emit_row(const ProbeArgs & a, const OutCols & o,
         }
 }
 
-// Column pass over the chunk's match list: thread i writes output row
-// base + i, so every store of a column is coalesced; the loads are gathers
-// through the list (build rows) or nearly sequential (probe rows).
+// Column pass of one warp over its match list: lane l writes output rows
+// base + l, base + l + 32, ... (coalesced); eight loads are in flight per
+// lane before its stores.
 template <class T, bool kBuild>
-__device__ __forceinline__ void column_pass(const void * src_v, void * dst_v, const uint32_t * idx, uint32_t n, uint64_t base)
+__device__ __forceinline__ void column_pass(const void * src_v, void * dst_v, const uint32_t * idx, uint32_t n, uint64_t base, uint32_t lane)
 {
     const T * src = static_cast<const T *>(src_v);
     T * dst = static_cast<T *>(dst_v) + base;
-    uint32_t i = threadIdx.x;
-    for (; i + 3 * kPNT < n; i += 4 * kPNT)
+    uint32_t i = lane;
+    for (; i + 7 * 32 < n; i += 8 * 32)
     {
-        T v0, v1, v2, v3;
-        if (kBuild)
-        {
-            v0 = __ldg(src + idx[i]);
-            v1 = __ldg(src + idx[i + kPNT]);
-            v2 = __ldg(src + idx[i + 2 * kPNT]);
-            v3 = __ldg(src + idx[i + 3 * kPNT]);
-        }
-        else
-        {
-            v0 = __ldcs(src + idx[i]);
-            v1 = __ldcs(src + idx[i + kPNT]);
-            v2 = __ldcs(src + idx[i + 2 * kPNT]);
-            v3 = __ldcs(src + idx[i + 3 * kPNT]);
-        }
-        __stcs(dst + i, v0);
-        __stcs(dst + i + kPNT, v1);
-        __stcs(dst + i + 2 * kPNT, v2);
-        __stcs(dst + i + 3 * kPNT, v3);
+        T v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            v[u] = kBuild ? __ldg(src + idx[i + u * 32]) : __ldcs(src + idx[i + u * 32]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+            __stcs(dst + i + u * 32, v[u]);
     }
-    for (; i < n; i += kPNT)
+    for (; i < n; i += 32)
         __stcs(dst + i, kBuild ? __ldg(src + idx[i]) : __ldcs(src + idx[i]));
 }
 
 template <bool kBuild>
-__device__ __forceinline__ void columns_pass(const Cols & src, void * const * dst, const uint32_t * idx, uint32_t n, uint64_t base)
+__device__ __forceinline__ void columns_pass(const Cols & src, void * const * dst, const uint32_t * idx, uint32_t n, uint64_t base, uint32_t lane)
 {
 #pragma unroll 1
     for (uint32_t c = 0; c < src.n; ++c)
         switch (src.width[c])
         {
-            case 1: column_pass<uint8_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
-            case 2: column_pass<uint16_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
-            case 4: column_pass<uint32_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
-            case 8: column_pass<uint64_t, kBuild>(src.col[c], dst[c], idx, n, base); break;
-            default: column_pass<uint4, kBuild>(src.col[c], dst[c], idx, n, base); break;
+            case 1: column_pass<uint8_t, kBuild>(src.col[c], dst[c], idx, n, base, lane); break;
+            case 2: column_pass<uint16_t, kBuild>(src.col[c], dst[c], idx, n, base, lane); break;
+            case 4: column_pass<uint32_t, kBuild>(src.col[c], dst[c], idx, n, base, lane); break;
+            case 8: column_pass<uint64_t, kBuild>(src.col[c], dst[c], idx, n, base, lane); break;
+            default: column_pass<uint4, kBuild>(src.col[c], dst[c], idx, n, base, lane); break;
         }
 }
 
-// Matches of one chunk, compacted in shared memory (the flat
-// (probe_idx, build_ref) arrays of probeOneBlock, plus the key).
-template <bool kDup>
-struct MatchList
-{
-    static constexpr uint32_t kCap = kDup ? 2 * kChunk : kChunk;
-    uint64_t key[kCap];
-    uint32_t brow[kCap];
-    uint32_t prow[kCap];
-};
-
-// kDup: some build key repeats, so rows may have several matches (chain
-// walks); without it every matched row yields exactly one output row and the
-// kernel carries no chain code at all.
-// Chunk status words for the decoupled look-back that places each chunk's
-// output rows: flag in the top two bits, row count below.
-constexpr unsigned long long kFlagAgg = 1ull << 62;  // the chunk's own total
-constexpr unsigned long long kFlagIncl = 2ull << 62; // total of chunks 0..c
-constexpr unsigned long long kValMask = (1ull << 62) - 1;
-
-// Publishes chunk c's total and finds the rows of all earlier chunks.  Only
-// thread 0 of the CTA calls it.  Chunks are taken in increasing order by
-// co-resident CTAs (cooperative launch), so the lowest unfinished chunk
-// never waits; every wait is still bounded.
-__device__ __forceinline__ unsigned long long chunk_base(unsigned long long * status, uint64_t c, uint32_t total, int * err)
-{
-    if (c == 0)
-    {
-        atomicExch(status, kFlagIncl | total);
-        return 0;
-    }
-    atomicExch(status + c, kFlagAgg | total);
-    unsigned long long acc = 0;
-    uint64_t j = c - 1;
-    for (uint32_t spins = 0;;)
-    {
-        const unsigned long long st = *reinterpret_cast<volatile unsigned long long *>(status + j);
-        if (st & kFlagIncl)
-        {
-            acc += st & kValMask;
-            break;
-        }
-        if (st & kFlagAgg)
-        {
-            acc += st & kValMask;
-            --j; // chunk 0 always holds an inclusive value
-            continue;
-        }
-        if (++spins >= kWaitLimit)
-        {
-            atomicExch(err, 2);
-            return ~0ull;
-        }
-    }
-    atomicExch(status + c, kFlagIncl | (acc + total));
-    return acc;
-}
-
+// Lookups: per probe row its head build row (kNoMatch when the key is
+// absent), per warp chunk its number of output rows.
 template <int kMode, bool kDup>
-__global__ void __launch_bounds__(kPNT) k_probe(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o,
-                                                unsigned long long * __restrict__ status, uint64_t out_cap, int count_only,
-                                                int * __restrict__ err)
+__global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
+                                                       uint32_t * __restrict__ counts)
 {
-    extern __shared__ __align__(16) uint8_t smem_raw[];
-    MatchList<kDup> & ml = *reinterpret_cast<MatchList<kDup> *>(smem_raw);
-    __shared__ uint32_t warp_tot[kPWarps];
-    __shared__ uint32_t chunk_total;
-    __shared__ unsigned long long sh_base;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
     const uint32_t shift = 64u - a.leaf_bits;
     const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
     const uint64_t ucap = 1ull << ulog;
-    for (uint64_t chunk = blockIdx.x; chunk < n_chunks; chunk += gridDim.x)
+    for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
     {
-        const uint64_t row0 = chunk * kChunk + warp * 32 + lane; // + k * kPNT
+        const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
         uint64_t key[kPRPT];
-        uint32_t brow[kPRPT];
-        uint32_t valid = 0, dup = 0;
-        // ---- lookups: eight independent key -> table chains per thread
+        uint32_t live = 0;
 #pragma unroll
         for (int k = 0; k < kPRPT; ++k)
         {
-            const uint64_t row = row0 + (uint64_t)k * kPNT;
+            const uint64_t row = row0 + (uint64_t)k * 32;
             key[k] = 0;
-            brow[k] = 0;
             if (row < a.probe_rows)
             {
                 key[k] = __ldcs(a.probe.keys + row);
+                live |= 1u << k;
+            }
+        }
+        uint32_t total = 0;
+        // four directory loads (per-leaf tables), four first-cell loads,
+        // then the comparisons: four table requests in flight per lane
+#pragma unroll
+        for (int g = 0; g < kPRPT; g += 4)
+        {
+            ulonglong2 mv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                mv[u] = make_ulonglong2(0ull, 0ull);
+                if (kMode != kLeafUniform && (live >> (g + u) & 1u))
+                    mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
+            }
+            ulonglong2 cell[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                const int k = g + u;
+                cell[u] = make_ulonglong2(0ull, INVALID_REF);
+                if (!(live >> k & 1u))
+                    continue;
                 const uint64_t h = int_hash64(key[k]);
-                const uint32_t leaf = (uint32_t)(h >> shift);
-                uint64_t head;
                 if (kMode == kLeafUniform)
-                {
-                    head = table_find(a.cells + ((uint64_t)leaf << ulog), ucap, h, key[k]);
-                    dup |= (kDup ? 1u : 0u) << k;
-                }
-                else
-                {
-                    const ulonglong2 mv = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + leaf));
-                    const uint32_t log2cap = (uint32_t)(mv.y >> 32) & 0xffu;
-                    const uint32_t has = (uint32_t)(mv.y >> 40) & 0xffu;
-                    if (kDup)
-                        dup |= (uint32_t)((mv.y >> 48) & 1u) << k;
-                    head = has ? table_find(a.cells + mv.x, 1ull << log2cap, h, key[k]) : INVALID_REF;
-                }
-                if (ref_valid(head))
-                {
-                    valid |= 1u << k;
-                    brow[k] = build_row_of<kMode>(head, a);
-                }
+                    cell[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + (h & (ucap - 1))));
+                else if ((mv[u].y >> 40) & 0xffu)
+                    cell[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.cells + mv[u].x + (h & ((1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)) - 1))));
             }
-        }
-        dup &= valid;
-        // ---- counts and placement: warp scans, one combine per chunk
-        uint32_t excl[kPRPT];
-        uint32_t running = 0;
 #pragma unroll
-        for (int k = 0; k < kPRPT; ++k)
-        {
-            uint32_t c = valid >> k & 1u;
-            if (kDup && (dup >> k & 1u))
-                c = chain_length(brow[k], a, kMode == kChj);
-            uint32_t x = c;
-#pragma unroll
-            for (int d = 1; d < 32; d <<= 1)
+            for (int u = 0; u < 4; ++u)
             {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
-                if (lane >= (uint32_t)d)
-                    x += y;
+                const int k = g + u;
+                uint32_t brow = kNoMatch;
+                if (ref_valid(cell[u].y))
+                {
+                    uint64_t head = cell[u].y;
+                    if (cell[u].x != key[k])
+                    {
+                        const uint64_t h = int_hash64(key[k]);
+                        if (kMode == kLeafUniform)
+                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, (h & (ucap - 1)) + 1, key[k]);
+                        else
+                        {
+                            const uint64_t c = 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu);
+                            head = table_find_from(a.cells + mv[u].x, c, (h & (c - 1)) + 1, key[k]);
+                        }
+                    }
+                    if (ref_valid(head))
+                    {
+                        brow = build_row_of<kMode>(head, a);
+                        const bool leaf_dup = kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
+                        total += (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
+                    }
+                }
+                if (live >> k & 1u)
+                    heads[row0 + (uint64_t)k * 32] = brow;
             }
-            excl[k] = running + x - c;
-            running += __shfl_sync(0xffffffffu, x, 31);
         }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            total += __shfl_xor_sync(0xffffffffu, total, o);
         if (lane == 0)
-            warp_tot[warp] = running;
-        __syncthreads();
-        if (threadIdx.x == 0)
-        {
-            uint32_t acc = 0;
-            for (int w = 0; w < kPWarps; ++w)
-            {
-                const uint32_t t = warp_tot[w];
-                warp_tot[w] = acc;
-                acc += t;
-            }
-            chunk_total = acc;
-            sh_base = chunk_base(status, chunk, acc, err);
-        }
-        __syncthreads();
-        if (count_only || sh_base == ~0ull)
-            continue;
-        const uint64_t base = sh_base;
-        const uint32_t total = chunk_total;
-        const uint32_t wbase = warp_tot[warp];
-        // ---- compact the matches into the chunk's list
+            counts[chunk] = total;
+    }
+}
+
+// The projection walks a warp chunk in halves of kPH rounds (to bound
+// registers); the output offset carries over from one half to the next.
+constexpr int kPH = 4;
+
+// One column over a lane's single-match rows of a half: four loads, then
+// four stores.  Output row of round k is base + rel[k].
+template <class T>
+__device__ __forceinline__ void project_column(const void * src_v, void * dst_v, const uint32_t (&sidx)[kPH], uint64_t base,
+                                               const uint32_t (&rel)[kPH], uint32_t one, bool gather)
+{
+    const T * src = static_cast<const T *>(src_v);
+    T * dst = static_cast<T *>(dst_v) + base;
+    T v[kPH];
 #pragma unroll
-        for (int k = 0; k < kPRPT; ++k)
+    for (int u = 0; u < kPH; ++u)
+        if (one >> u & 1u)
+            v[u] = gather ? __ldg(src + sidx[u]) : __ldcs(src + sidx[u]);
+#pragma unroll
+    for (int u = 0; u < kPH; ++u)
+        if (one >> u & 1u)
+            __stcs(dst + rel[u], v[u]);
+}
+
+// All output columns, one switch instance for the loop.
+__device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t (&brow)[kPH], const uint32_t (&prow)[kPH], uint64_t base,
+                                            const uint32_t (&rel)[kPH], uint32_t one)
+{
+#pragma unroll 1
+    for (uint32_t c = 0; c < pc.n; ++c)
+    {
+        const bool g = pc.by_build[c] != 0;
+        uint32_t idx[kPH];
+#pragma unroll
+        for (int u = 0; u < kPH; ++u)
+            idx[u] = g ? brow[u] : prow[u];
+        switch (pc.width[c])
         {
-            if (!(valid >> k & 1u))
-                continue;
-            uint32_t i = wbase + excl[k];
-            const uint32_t prow = (uint32_t)(row0 + (uint64_t)k * kPNT);
-            uint32_t b = brow[k];
-            for (;;)
-            {
-                if (i < MatchList<kDup>::kCap)
-                {
-                    ml.key[i] = key[k];
-                    ml.brow[i] = b;
-                    ml.prow[i] = prow;
-                }
-                else if (base + i < out_cap) // past the list: written directly
-                    emit_row(a, o, b, key[k], prow, base + i);
-                if (!kDup || !(dup >> k & 1u))
-                    break;
-                const uint64_t r = __ldg(a.next + b);
-                if (!ref_valid(r))
-                    break;
-                b = build_row_of<kMode>(r, a);
-                ++i;
-            }
+            case 1: project_column<uint8_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 2: project_column<uint16_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 4: project_column<uint32_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 8: project_column<uint64_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            default: project_column<uint4>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
         }
-        __syncthreads();
-        // ---- column passes: key, build payloads, probe payloads
-        uint32_t n = min(total, MatchList<kDup>::kCap);
-        if (base + n > out_cap)
-            n = base >= out_cap ? 0u : (uint32_t)(out_cap - base);
-        for (uint32_t i = threadIdx.x; i < n; i += kPNT)
-            __stcs(o.keys + base + i, ml.key[i]);
-        columns_pass<true>(a.build, o.left, ml.brow, n, base);
-        columns_pass<false>(a.probe, o.right, ml.prow, n, base);
-        __syncthreads(); // the list is rewritten by the next chunk
+    }
+}
+
+// Projection: warp chunk c writes its output rows from offs[c] on.  Rows
+// with one match are written column by column; rows of duplicate keys
+// write their chains row by row.
+template <int kMode, bool kDup>
+__global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o,
+                                                        const __grid_constant__ ProjCols pc, const uint32_t * __restrict__ heads,
+                                                        const uint32_t * __restrict__ offs, uint64_t out_cap)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
+    for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
+    {
+        uint64_t base = offs[chunk];
+#pragma unroll 1
+        for (int half = 0; half < kPRPT / kPH; ++half)
+        {
+            const uint64_t row0 = chunk * kWChunk + (uint64_t)half * kPH * 32 + lane;
+            uint32_t brow[kPH], prow[kPH], cnt[kPH];
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                const uint64_t row = row0 + (uint64_t)k * 32;
+                prow[k] = (uint32_t)row;
+                brow[k] = row < a.probe_rows ? __ldcs(heads + row) : kNoMatch;
+            }
+            uint32_t one = 0, multi = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                cnt[k] = brow[k] != kNoMatch ? 1u : 0u;
+                if (kDup && cnt[k])
+                {
+                    const uint64_t nx = __ldg(a.next + brow[k]);
+                    if (ref_valid(nx))
+                    {
+                        cnt[k] = chain_length(brow[k], a, kMode == kChj);
+                        multi |= 1u << k;
+                    }
+                }
+                if (cnt[k] == 1u)
+                    one |= 1u << k;
+            }
+            // placement: warp scan per round, round-major
+            uint32_t rel[kPH];
+            uint32_t running = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                uint32_t x = cnt[k];
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1)
+                {
+                    const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                    if (lane >= (uint32_t)d)
+                        x += y;
+                }
+                rel[k] = running + x - cnt[k];
+                running += __shfl_sync(0xffffffffu, x, 31);
+                if (base + rel[k] >= out_cap)
+                    one &= ~(1u << k);
+            }
+            // key column (the probe key), build payloads, probe payloads
+            project_all(pc, brow, prow, base, rel, one);
+            if (kDup && multi)
+            {
+#pragma unroll 1
+                for (int k = 0; k < kPH; ++k)
+                    if (multi >> k & 1u)
+                    {
+                        const uint64_t key = a.probe.keys[prow[k]];
+                        uint32_t b = brow[k];
+                        for (uint64_t p = base + rel[k]; p < out_cap; ++p)
+                        {
+                            emit_row(a, o, b, key, prow[k], p);
+                            const uint64_t r = __ldg(a.next + b);
+                            if (!ref_valid(r))
+                                break;
+                            b = build_row_of<kMode>(r, a);
+                        }
+                    }
+            }
+            base += running;
+        }
     }
 }
 } // namespace
 
-uint64_t probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, phj_output * out, bool count_only, const char * name)
+static ProjCols proj_cols(const ProbeArgs & a, const OutCols & o)
 {
-    const uint64_t n_chunks = ceil_div(a.probe_rows, kChunk);
-    unsigned long long * status = s.get<unsigned long long>(n_chunks + 1);
-    PHJ_CUDA(cudaMemsetAsync(status, 0, (n_chunks + 1) * sizeof(unsigned long long), ctx->stream));
-    OutCols o{};
-    uint64_t cap = 0;
-    if (out)
+    ProjCols pc{};
+    uint32_t n = 0;
+    pc.src[n] = a.probe.keys;
+    pc.dst[n] = o.keys;
+    pc.width[n] = 8;
+    pc.by_build[n++] = 0;
+    for (uint32_t c = 0; c < a.build.n; ++c)
     {
-        o.keys = out->keys;
-        for (uint32_t c = 0; c < out->left.n_payloads; ++c)
-            o.left[c] = out->lcol[c];
-        for (uint32_t c = 0; c < out->right.n_payloads; ++c)
-            o.right[c] = out->rcol[c];
-        cap = out->cap;
+        pc.src[n] = a.build.col[c];
+        pc.dst[n] = o.left[c];
+        pc.width[n] = a.build.width[c];
+        pc.by_build[n++] = 1;
     }
-    const int mode = a.chj ? kChj : (a.uniform_log2cap >= 0 ? kLeafUniform : kLeafMeta);
-    auto kern = a.any_dup ? (mode == kChj ? k_probe<kChj, true> : mode == kLeafUniform ? k_probe<kLeafUniform, true> : k_probe<kLeafMeta, true>)
-                          : (mode == kChj ? k_probe<kChj, false> : mode == kLeafUniform ? k_probe<kLeafUniform, false> : k_probe<kLeafMeta, false>);
-    const size_t smem = a.any_dup ? sizeof(MatchList<true>) : sizeof(MatchList<false>);
-    PHJ_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    for (uint32_t c = 0; c < a.probe.n; ++c)
+    {
+        pc.src[n] = a.probe.col[c];
+        pc.dst[n] = o.right[c];
+        pc.width[n] = a.probe.width[c];
+        pc.by_build[n++] = 0;
+    }
+    pc.n = n;
+    return pc;
+}
+
+template <int kMode, bool kDup>
+static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, uint32_t * heads, uint32_t * counts, uint64_t cap, bool lookup,
+                         const char * name, uint64_t bytes)
+{
     int per_sm = 0;
-    PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kPNT, smem));
-    // Every CTA must be resident (the look-back waits on other CTAs'
-    // chunks): a cooperative launch of at most one wave.
-    const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(std::max<uint64_t>(n_chunks, 1), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
+    if (lookup)
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_lookup<kMode, kDup>, kPNT, 0));
+    else
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode, kDup>, kPNT, 0));
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const unsigned grid = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>(ceil_div(std::max<uint64_t>(n_chunks, 1), kPWarps), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
+    if (std::getenv("PHJ_DEBUG"))
+        std::fprintf(stderr, "[phj] %s: mode %d dup %d grid %u x %d threads, %d CTAs/SM, chunks %llu\n", name, kMode, (int)kDup, grid, kPNT, per_sm,
+                     (unsigned long long)n_chunks);
+    KTimer kt(ctx, name, a.probe_rows, bytes);
+    if (lookup)
+        k_probe_lookup<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
+    else
+        k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
+    PHJ_LAUNCHED(ctx, name);
+}
+
+template <int kMode>
+static void launch_probe_mode(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, uint32_t * heads, uint32_t * counts, uint64_t cap, bool lookup,
+                              const char * name, uint64_t bytes)
+{
+    if (a.any_dup)
+        launch_probe<kMode, true>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
+    else
+        launch_probe<kMode, false>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
+}
+
+static void launch_any(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, uint32_t * heads, uint32_t * counts, uint64_t cap, bool lookup,
+                       const char * name, uint64_t bytes)
+{
+    if (a.chj)
+        launch_probe_mode<kChj>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
+    else if (a.uniform_log2cap >= 0)
+        launch_probe_mode<kLeafUniform>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
+    else
+        launch_probe_mode<kLeafMeta>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
+}
+
+phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+{
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    uint32_t * heads = s.get<uint32_t>(a.probe_rows);
+    uint32_t * counts = s.get<uint32_t>(n_chunks + 1);
     uint64_t probe_row_bytes = 8, build_row_bytes = 0;
     for (uint32_t c = 0; c < a.probe.n; ++c)
         probe_row_bytes += a.probe.width[c];
     for (uint32_t c = 0; c < a.build.n; ++c)
         build_row_bytes += a.build.width[c];
-    {
-        KTimer kt(ctx, name, a.probe_rows, count_only ? a.probe_rows * 8 : a.probe_rows * probe_row_bytes);
-        int co = count_only ? 1 : 0;
-        ProbeArgs aa = a;
-        void * args[] = {&aa, &o, &status, &cap, &co, &ctx->d_err};
-        PHJ_CUDA(cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(kPNT), args, smem, ctx->stream));
-        PHJ_LAUNCHED(ctx, name);
-    }
-    unsigned long long last = 0;
-    if (n_chunks)
-        PHJ_CUDA(cudaMemcpyAsync(&last, status + n_chunks - 1, sizeof(last), cudaMemcpyDeviceToHost, ctx->stream));
+    launch_any(ctx, a, nullptr, heads, counts, 0, true, "probe_lookup", a.probe_rows * (8 + 4));
+    scan_u32(ctx, s, counts, counts, n_chunks);
+    uint32_t total = 0;
+    PHJ_CUDA(cudaMemcpyAsync(&total, counts + n_chunks, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
-    const uint64_t rows = last & kValMask;
-    // Algorithmic bytes of the timed launch, now that the output size is
-    // known: probe rows read + output rows (key + build + probe payloads).
-    if (!count_only && !ctx->records.empty())
-        ctx->records.back().bytes += rows * (8 + build_row_bytes + (probe_row_bytes - 8));
-    return rows;
+    phj_output * out = new_output(ctx, left, right, total);
+    out->rows = total;
+    OutCols o{};
+    o.keys = out->keys;
+    for (uint32_t c = 0; c < out->left.n_payloads; ++c)
+        o.left[c] = out->lcol[c];
+    for (uint32_t c = 0; c < out->right.n_payloads; ++c)
+        o.right[c] = out->rcol[c];
+    try
+    {
+        // algorithmic bytes: head array + output rows (key, build payloads,
+        // probe payloads)
+        launch_any(ctx, a, &o, heads, counts, total, false, "probe_project",
+                   a.probe_rows * 4 + (uint64_t)total * (8 + build_row_bytes + (probe_row_bytes - 8)));
+    }
+    catch (...)
+    {
+        free_output(ctx, out);
+        throw;
+    }
+    return out;
 }
 
 } // namespace phjg

@@ -20,7 +20,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libphj_gpu.so")
+LIB_PATH = os.environ.get("PHJ_GPU_LIB") or os.path.join(HERE, "libphj_gpu.so")
 MAX_PAYLOADS = 8
 
 # PayloadType codes, src/Types.h:23-30

@@ -45,7 +45,7 @@ def test_kernel_times_and_launch_count(ctx):
     out, res = ctx.run_phj_pure(b, p, [6, 6])
     assert ctx.launch_count() > n0
     names = [k["name"] for k in ctx.kernel_times()]
-    assert "probe_join" in names and "build_scatter" in names
+    assert "probe_lookup" in names and "probe_project" in names and "build_scatter" in names
     assert all(k["ms"] >= 0 for k in ctx.kernel_times())
     fp = out.fingerprint()
     hb, hp = b.download(), p.download()
