@@ -479,6 +479,7 @@ phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const p
         probe_row_bytes += a.probe.width[c];
     for (uint32_t c = 0; c < a.build.n; ++c)
         build_row_bytes += a.build.width[c];
+    // algorithmic bytes: probe keys read, head array written
     launch_any(ctx, a, nullptr, heads, counts, 0, true, "probe_lookup", a.probe_rows * (8 + 4));
     scan_u32(ctx, s, counts, counts, n_chunks);
     uint32_t total = 0;
@@ -494,10 +495,10 @@ phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const p
         o.right[c] = out->rcol[c];
     try
     {
-        // algorithmic bytes: head array + output rows (key, build payloads,
-        // probe payloads)
+        // algorithmic bytes: the head array, the probe key and payloads of
+        // every output row (read), the output rows (written)
         launch_any(ctx, a, &o, heads, counts, total, false, "probe_project",
-                   a.probe_rows * 4 + (uint64_t)total * (8 + build_row_bytes + (probe_row_bytes - 8)));
+                   a.probe_rows * 4 + (uint64_t)total * probe_row_bytes + (uint64_t)total * (8 + build_row_bytes + (probe_row_bytes - 8)));
     }
     catch (...)
     {
