@@ -157,8 +157,42 @@ uint32_t max_width(const Cols & c)
     return w;
 }
 
+// Moves an output to a larger capacity, keeping its first `keep` rows.
+void grow_output(phj_ctx * ctx, phj_output * o, uint64_t cap, uint64_t keep)
+{
+    phj_output * n = new_output(ctx, o->left, o->right, cap);
+    PHJ_CUDA(cudaMemcpyAsync(n->keys, o->keys, keep * 8, cudaMemcpyDeviceToDevice, ctx->stream));
+    for (uint32_t c = 0; c < o->left.n_payloads; ++c)
+        PHJ_CUDA(cudaMemcpyAsync(n->lcol[c], o->lcol[c], keep * payload_width(o->left.types[c]), cudaMemcpyDeviceToDevice, ctx->stream));
+    for (uint32_t c = 0; c < o->right.n_payloads; ++c)
+        PHJ_CUDA(cudaMemcpyAsync(n->rcol[c], o->rcol[c], keep * payload_width(o->right.types[c]), cudaMemcpyDeviceToDevice, ctx->stream));
+    std::swap(*o, *n);
+    free_output(ctx, n);
+}
+
 namespace
 {
+// Non-empty first-pass buckets of a probe batch: each is one refinement
+// (its rows go on to leaf depth).
+__global__ void k_count_nonempty(const uint32_t * __restrict__ off, uint32_t n, unsigned long long * __restrict__ ctr)
+{
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool ne = i < n && off[i + 1] > off[i];
+    const uint32_t m = __ballot_sync(0xffffffffu, ne);
+    if ((threadIdx.x & 31) == 0 && m)
+        atomicAdd(ctr, (unsigned long long)__popc(m));
+}
+
+// Columns of a table advanced by `r0` rows.
+Cols cols_from(const Cols & c, uint64_t r0)
+{
+    Cols o = c;
+    if (o.keys)
+        o.keys += r0;
+    for (uint32_t i = 0; i < c.n; ++i)
+        o.col[i] = static_cast<uint8_t *>(c.col[i]) + r0 * c.width[i];
+    return o;
+}
 template <class F>
 phj_status guard(phj_ctx * ctx, F && f)
 {
@@ -500,6 +534,150 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     *out = o;
 }
 
+// PHJ (BEP).  The build side is shuffled to full leaf depth and its leaf
+// tables are planned but left NOT_BUILT; the probe side streams through in
+// batches of at most the byte budget.  Each batch is scattered by the first
+// radix pass (probe shuffle), then probed against the leaf tables, the first
+// warp to reach a leaf building its table.  A batch's probe drains every
+// leaf it touched, which is the device form of the reference's eviction
+// (src/PHJBep.cpp:113-790).
+static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P, const std::vector<uint32_t> & bits, uint64_t budget_mib,
+                        phj_output ** out, phj_bep_result * res)
+{
+    begin_run(ctx);
+    Scratch s(ctx);
+    uint32_t total_bits = 0;
+    for (uint32_t b : bits)
+        total_bits += b;
+    const uint32_t n_leaves = 1u << total_bits;
+    cudaEvent_t ev[3], eb[3];
+    for (auto & e : ev)
+        e = take_event(ctx);
+    for (auto & e : eb)
+        e = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+
+    // -------- BUILD SHUFFLE, full leaf depth (src/PHJBep.cpp:128-141) --------
+    const Cols bin = cols_of(B);
+    const Cols bpart = alloc_cols_like(s, B.schema, B.rows);
+    const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
+    uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
+    radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+
+    // -------- BUILD: table layout only; cells are built on first use --------
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(B.rows);
+    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt, true);
+    if (ctx->test_stuck_leaf >= 0 && (uint64_t)ctx->test_stuck_leaf < n_leaves)
+    {
+        const uint32_t building = 1;
+        PHJ_CUDA(cudaMemcpyAsync(lt.state + ctx->test_stuck_leaf, &building, sizeof(building), cudaMemcpyHostToDevice, ctx->stream));
+        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
+
+    unsigned long long * ctr = s.get<unsigned long long>(4);
+    uint32_t * epoch = s.get<uint32_t>(n_leaves);
+    PHJ_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(epoch, 0, (size_t)n_leaves * sizeof(uint32_t), ctx->stream));
+
+    ProbeArgs a{};
+    a.build = payload_cols(bpart);
+    a.meta = lt.meta;
+    a.cells = lt.cells;
+    a.next = lt.next;
+    a.leaf_bits = total_bits;
+    a.chj = 0;
+    a.any_dup = 1;
+    a.uniform_log2cap = lt.uniform_log2cap;
+    a.leaf_state = lt.state;
+    a.leaf_off = leaf_off;
+    a.build_keys = bpart.keys;
+    a.leaf_epoch = epoch;
+    a.wait_limit_ns = (uint64_t)ctx->wait_limit_ms * 1000000ull;
+    a.bep_ctr = ctr;
+
+    // -------- PROBE: budget-sized batches --------
+    const uint64_t row_bytes = 8 + schema_bytes(P.schema);
+    const uint64_t budget_rows = (budget_mib << 20) / row_bytes;
+    const uint64_t batch_rows = std::min<uint64_t>(std::max<uint64_t>(P.rows, 1), std::max<uint64_t>(4096, budget_rows & ~uint64_t(255)));
+    const uint32_t p1 = 1u << bits[0];
+    const Cols pin = cols_of(P);
+    const Cols ppart = alloc_cols_like(s, P.schema, batch_rows);
+    const Cols ptmp = bits[0] > 11 ? alloc_cols_like(s, P.schema, batch_rows) : ppart;
+    uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
+    uint32_t * heads = s.get<uint32_t>(batch_rows);
+    uint32_t * counts = s.get<uint32_t>(probe_chunks(batch_rows) + 1);
+    phj_output * o = nullptr;
+    uint64_t total = 0, peak_rows = 0;
+    float t_shuffle = 0.f, t_probe = 0.f;
+    try
+    {
+        uint32_t e = 1;
+        for (uint64_t r0 = 0; r0 < P.rows; r0 += batch_rows, ++e)
+        {
+            const uint64_t n_b = std::min(batch_rows, P.rows - r0);
+            peak_rows = std::max(peak_rows, n_b);
+            Scratch sb(ctx);
+            PHJ_CUDA(cudaEventRecord(eb[0], ctx->stream));
+            radix_partition(ctx, sb, cols_from(pin, r0), n_b, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            k_count_nonempty<<<(unsigned)ceil_div(p1, 256), 256, 0, ctx->stream>>>(poff, p1, ctr + 3);
+            PHJ_LAUNCHED(ctx, "count_refinements");
+            PHJ_CUDA(cudaEventRecord(eb[1], ctx->stream));
+            a.probe = ppart;
+            a.probe_rows = n_b;
+            a.epoch = e;
+            const uint64_t rows = probe_lookup(ctx, sb, a, heads, counts);
+            check_device_error(ctx);
+            if (!o)
+            {
+                // first batch: extrapolate the output size over the stream
+                const uint64_t est = (uint64_t)((double)rows * (double)P.rows / (double)n_b * 1.0625) + 4096;
+                o = new_output(ctx, B.schema, P.schema, std::max(est, rows));
+            }
+            else if (total + rows > o->cap)
+                grow_output(ctx, o, std::max(o->cap * 2, total + rows), total);
+            probe_project(ctx, a, o, total, heads, counts, rows);
+            total += rows;
+            PHJ_CUDA(cudaEventRecord(eb[2], ctx->stream));
+            PHJ_CUDA(cudaEventSynchronize(eb[2]));
+            t_shuffle += event_ms(eb[0], eb[1]);
+            t_probe += event_ms(eb[1], eb[2]);
+        }
+        if (!o)
+            o = new_output(ctx, B.schema, P.schema, 0);
+        o->rows = total;
+        PHJ_CUDA(cudaEventRecord(eb[0], ctx->stream));
+        PHJ_CUDA(cudaEventSynchronize(eb[0]));
+        check_device_error(ctx);
+    }
+    catch (...)
+    {
+        free_output(ctx, o);
+        throw;
+    }
+    if (res)
+    {
+        unsigned long long c[4] = {};
+        PHJ_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
+        const float bs = event_ms(ev[0], ev[1]), bd = event_ms(ev[1], ev[2]), e2e = event_ms(ev[0], eb[0]);
+        fill_phase(res->build_shuffle, bs, B.rows);
+        fill_phase(res->build, bd, B.rows);
+        fill_phase(res->probe_shuffle, t_shuffle, P.rows);
+        fill_phase(res->probe, t_probe, P.rows);
+        fill_phase(res->eviction_overhead, std::max(0.f, e2e - bs - bd - t_shuffle - t_probe), P.rows);
+        res->e2e_wall_ms = e2e;
+        res->peak_mem_bytes = ctx->peak_bytes;
+        res->bep_budget_mib = budget_mib;
+        res->bep_evictions = c[2];
+        res->bep_refinements = c[3];
+        res->bep_peak_bytes = peak_rows * row_bytes;
+        res->bep_build_skip_retries = c[1];
+    }
+    *out = o;
+}
+
 } // namespace phjg
 
 using namespace phjg;
@@ -605,6 +783,10 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->probe_materialize = (int)value;
     else if (std::strcmp(name, "time_kernels") == 0)
         ctx->time_kernels = value != 0;
+    else if (std::strcmp(name, "wait_limit_ms") == 0 && value >= 1 && value <= 60000)
+        ctx->wait_limit_ms = value;
+    else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
+        ctx->test_stuck_leaf = value;
     else
         return PHJ_ERR_INVALID_ARGUMENT;
     return PHJ_OK;
@@ -816,13 +998,13 @@ phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_tab
     if (!ctx || !out)
         return PHJ_ERR_INVALID_ARGUMENT;
     *out = nullptr;
-    (void)bep_budget_mib;
-    (void)workers;
-    (void)result;
+    (void)workers; // the reference's threads; one device-wide batch replaces the per-worker split
     return guard(ctx, [&] {
-        (void)check_bits(pass_bits, n_passes);
+        const std::vector<uint32_t> bits = check_bits(pass_bits, n_passes);
         check_sides(build, probe);
-        throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) device scheme not built yet");
+        if (bep_budget_mib == 0 || bep_budget_mib > (1ull << 30))
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "bep_budget_mib must be in [1, 2^30]");
+        run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
     });
 }
 

@@ -173,7 +173,23 @@ void set_build_smem_limits(int smem_optin)
     PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
 }
 
-void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves, LeafTables & lt)
+// Lazy layout (PHJ/BEP): the directory says where each leaf's table lives;
+// the cells are built on first use by the probe (state NOT_BUILT).
+__global__ void k_leaf_plan(const uint32_t * __restrict__ leaf_off, const uint32_t * __restrict__ table_off, int ulog, uint32_t n_leaves,
+                            LeafMeta * __restrict__ meta)
+{
+    const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
+    if (l >= n_leaves)
+        return;
+    const uint32_t r0 = leaf_off[l], r = leaf_off[l + 1] - r0;
+    const uint64_t t0 = ulog >= 0 ? ((uint64_t)l << ulog) : table_off[l];
+    const uint64_t cap = ulog >= 0 ? (1ull << ulog) : table_off[l + 1] - t0;
+    (void)r;
+    meta[l] = LeafMeta{t0, r0, cap ? (uint8_t)log2u(cap) : (uint8_t)0, (uint8_t)(cap != 0), 1, 0};
+}
+
+void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves, LeafTables & lt,
+                       bool lazy)
 {
     uint32_t * caps = s.get<uint32_t>(n_leaves + 1);
     uint32_t * table_off = s.get<uint32_t>(n_leaves + 1);
@@ -197,6 +213,15 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     lt.total_cells = uniform ? uniform_cells : host[1];
     lt.meta = s.get<LeafMeta>(n_leaves);
     lt.cells = s.get<Cell>(lt.total_cells);
+    if (lazy)
+    {
+        lt.state = s.get<uint32_t>(n_leaves);
+        PHJ_CUDA(cudaMemsetAsync(lt.state, 0, (size_t)n_leaves * sizeof(uint32_t), ctx->stream));
+        k_leaf_plan<<<(unsigned)ceil_div(n_leaves, 256), 256, 0, ctx->stream>>>(leaf_off, table_off, lt.uniform_log2cap, n_leaves, lt.meta);
+        PHJ_LAUNCHED(ctx, "leaf_plan");
+        lt.any_dup = 1; // unknown until the tables are built: chains are followed
+        return;
+    }
     const uint32_t smem_cells = (uint32_t)std::min<uint64_t>(max_cap, kSmemCellsMax);
     int * any_dup = reinterpret_cast<int *>(small + 1);
     {

@@ -86,6 +86,8 @@ struct phj_ctx
     int * d_err = nullptr; // device error word: bounded waits that gave up
     // Options (phj_ctx_set_int).
     int probe_materialize = -1; // -1 auto, 0 never, 1 always
+    int64_t wait_limit_ms = 1000; // bound of a device wait on another warp's work
+    int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
 };
 
 struct phj_table
@@ -201,11 +203,14 @@ struct LeafTables
     uint32_t max_rows = 0;
     int any_dup = 0;
     int uniform_log2cap = -1; // >= 0: every leaf table has 2^this cells at leaf << this
+    uint32_t * state = nullptr; // lazy build (PHJ/BEP): per leaf NOT_BUILT / BUILDING / BUILT
 };
 
-// Per-leaf tables over leaf-partitioned build rows (PHJ-PURE / PHJ).
+// Per-leaf tables over leaf-partitioned build rows (PHJ-PURE / PHJ).  With
+// `lazy` only the layout is planned; the probe builds each table on first
+// use (PHJ/BEP).
 void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves,
-                       LeafTables & lt);
+                       LeafTables & lt, bool lazy = false);
 // One global table of 2^slot_bits sub-tables namespaced by the top hash bits (CHJ).
 void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uint32_t slot_bits, LeafTables & lt);
 
@@ -224,9 +229,23 @@ struct ProbeArgs
     uint32_t uniform_block_rows;
     int any_dup;
     int uniform_log2cap;    // >= 0: PHJ leaf tables of uniform capacity (no directory lookup)
+    // Lazy leaf tables (PHJ/BEP): built by the first warp that needs one.
+    uint32_t * leaf_state;        // NOT_BUILT 0 -> BUILDING 1 -> BUILT 2 (3: BUILT, keys repeat)
+    const uint32_t * leaf_off;    // first build row of each leaf (n_leaves + 1)
+    const uint64_t * build_keys;  // leaf-partitioned build keys
+    uint32_t * leaf_epoch;        // last batch (1-based) that probed each leaf
+    uint32_t epoch;               // this batch
+    uint64_t wait_limit_ns;       // bound of a wait on a BUILDING leaf
+    unsigned long long * bep_ctr; // [0] tables built, [1] waits on BUILDING, [2] leaf evictions, [3] refinements
 };
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);
+// The two halves: lookups + chunk-offset scan (returns the output rows), and
+// the projection into `out` from row `out_base` on.
+uint64_t probe_chunks(uint64_t probe_rows);
+uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, uint32_t * heads, uint32_t * counts);
+void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_t out_base, const uint32_t * heads, const uint32_t * offs,
+                   uint64_t rows);
 phj_output * new_output(phj_ctx * ctx, const phj_schema & left, const phj_schema & right, uint64_t cap);
 void free_output(phj_ctx * ctx, phj_output * o);
 

@@ -75,13 +75,13 @@ __device__ __forceinline__ uint32_t build_row_of(uint64_t ref, const ProbeArgs &
 }
 
 // Linear probing from cell `pos` on (the first cell collided).
-__device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t cap, uint64_t pos, uint64_t key)
+__device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t cap, uint64_t pos, uint64_t key, bool coherent = false)
 {
     const uint64_t mask = cap - 1;
     pos &= mask;
     for (uint64_t step = 1; step < cap; ++step)
     {
-        const ulonglong2 c = __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
+        const ulonglong2 c = coherent ? __ldcg(reinterpret_cast<const ulonglong2 *>(cells + pos)) : __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
         if (!ref_valid(c.y))
             return INVALID_REF;
         if (c.x == key)
@@ -91,14 +91,15 @@ __device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t ca
     return INVALID_REF;
 }
 
-__device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj)
+__device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj, bool coherent = false)
 {
     uint32_t c = 1;
-    uint64_t r = __ldg(a.next + brow);
+    uint64_t r = coherent ? __ldcg(a.next + brow) : __ldg(a.next + brow);
     while (ref_valid(r))
     {
         ++c;
-        r = __ldg(a.next + (chj ? build_row_of<kChj>(r, a) : build_row_of<kLeafMeta>(r, a)));
+        const uint32_t b = chj ? build_row_of<kChj>(r, a) : build_row_of<kLeafMeta>(r, a);
+        r = coherent ? __ldcg(a.next + b) : __ldg(a.next + b);
     }
     return c;
 }
@@ -171,11 +172,143 @@ __device__ __forceinline__ void columns_pass(const Cols & src, void * const * ds
         }
 }
 
+// ---- lazy leaf tables (PHJ/BEP) --------------------------------------------
+// Leaf state: NOT_BUILT -> BUILDING -> BUILT (BUILT_DUP when a key repeats).
+constexpr uint32_t kNotBuilt = 0, kBuilding = 1, kBuilt = 2, kBuiltDup = 3;
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t * p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// The whole warp builds leaf L's table: clear the cells, insert the leaf's
+// build rows with 128-bit CAS, thread the next-chain.  Returns whether a
+// key repeats within the leaf.
+__device__ __noinline__ bool warp_build_leaf(const ProbeArgs & a, uint32_t L, uint32_t lane)
+{
+    const ulonglong2 mv = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + L));
+    if (!((mv.y >> 40) & 0xffu))
+        return false;
+    const uint64_t cap = 1ull << ((uint32_t)(mv.y >> 32) & 0xffu);
+    Cell * tab = const_cast<Cell *>(a.cells) + mv.x;
+    const uint32_t r0 = (uint32_t)mv.y;
+    const uint32_t r1 = __ldg(a.leaf_off + L + 1);
+    for (uint64_t i = lane; i < cap; i += 32)
+        reinterpret_cast<ulonglong2 *>(tab)[i] = make_ulonglong2(0ull, INVALID_REF);
+    __threadfence();
+    __syncwarp();
+    uint64_t * next = const_cast<uint64_t *>(a.next);
+    bool dup = false;
+    for (uint32_t r = r0 + lane; r < r1; r += 32)
+    {
+        const uint64_t k = __ldg(a.build_keys + r);
+        const uint64_t prev = table_insert<false>(tab, cap, int_hash64(k), k, make_ref(0, r));
+        next[r] = prev;
+        dup |= ref_valid(prev);
+    }
+    __threadfence();
+    return __any_sync(0xffffffffu, dup);
+}
+
+// Makes sure the leaves l[0..3] of a four-row group's live rows are built
+// and returns their states, two bits each.  The first warp to need a leaf
+// wins NOT_BUILT -> BUILDING, builds it and publishes BUILT; a warp that
+// finds it BUILDING waits, bounded by a wall-clock limit, and the wait is
+// counted.  Returns kStatesTimeout after a timeout (code 4 in *err).  Called
+// by the whole warp when some lane's leaf is not yet BUILT.
+constexpr uint32_t kStatesTimeout = 0xffffffffu;
+
+__device__ __noinline__ uint32_t ensure_built_slow(const ProbeArgs & a, uint32_t l0, uint32_t l1, uint32_t l2, uint32_t l3, uint32_t live4,
+                                                   uint32_t lane, int * err)
+{
+    const uint32_t leaf[4] = {l0, l1, l2, l3};
+    uint32_t st[4];
+    bool need[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+    {
+        st[u] = (live4 >> u & 1u) ? load_acquire(a.leaf_state + leaf[u]) : kBuilt;
+        need[u] = st[u] < kBuilt;
+    }
+#pragma unroll 1
+    for (int u = 0; u < 4; ++u)
+    {
+        for (uint32_t m = __ballot_sync(0xffffffffu, need[u]); m; m = __ballot_sync(0xffffffffu, need[u]))
+        {
+            const int src = __ffs(m) - 1;
+            const uint32_t L = __shfl_sync(0xffffffffu, leaf[u], src);
+            uint32_t won = 0;
+            if ((int)lane == src)
+                won = atomicCAS(a.leaf_state + L, kNotBuilt, kBuilding) == kNotBuilt;
+            won = __shfl_sync(0xffffffffu, won, src);
+            uint32_t ok = 1;
+            if (won)
+            {
+                const bool dup = warp_build_leaf(a, L, lane);
+                if ((int)lane == src)
+                {
+                    atomicExch(a.leaf_state + L, dup ? kBuiltDup : kBuilt);
+                    atomicAdd(a.bep_ctr + 0, 1ull);
+                }
+            }
+            else if ((int)lane == src && load_acquire(a.leaf_state + L) < kBuilt)
+            {
+                const uint64_t t0 = global_ns();
+                uint32_t spins = 0;
+                while (load_acquire(a.leaf_state + L) < kBuilt)
+                    if (++spins >= kWaitLimit || global_ns() - t0 > a.wait_limit_ns)
+                    {
+                        atomicExch(err, 4);
+                        ok = 0;
+                        break;
+                    }
+                atomicAdd(a.bep_ctr + 1, 1ull);
+            }
+            ok = __shfl_sync(0xffffffffu, ok, src);
+            if (!ok)
+                return kStatesTimeout;
+#pragma unroll
+            for (int v = 0; v < 4; ++v)
+                if (need[v])
+                {
+                    st[v] = load_acquire(a.leaf_state + leaf[v]);
+                    need[v] = st[v] < kBuilt;
+                }
+        }
+    }
+    return st[0] | st[1] << 2 | st[2] << 4 | st[3] << 6;
+}
+
+// The batch a leaf was last probed in; the first row of a new batch to
+// reach a leaf counts one eviction (the leaf's buffered rows are probed).
+__device__ __forceinline__ void note_leaf_batch(const ProbeArgs & a, uint32_t L)
+{
+    if (*reinterpret_cast<const volatile uint32_t *>(a.leaf_epoch + L) != a.epoch && atomicExch(a.leaf_epoch + L, a.epoch) != a.epoch)
+        atomicAdd(a.bep_ctr + 2, 1ull);
+}
+// Cell / next-chain loads: through the non-coherent read-only path when the
+// tables were finished by an earlier kernel, through L2 when this kernel
+// may build them (lazy).
+template <bool kLazy>
+__device__ __forceinline__ ulonglong2 load_cell(const Cell * p)
+{
+    return kLazy ? __ldcg(reinterpret_cast<const ulonglong2 *>(p)) : __ldg(reinterpret_cast<const ulonglong2 *>(p));
+}
+
 // Lookups: per probe row its head build row (kNoMatch when the key is
 // absent), per warp chunk its number of output rows.
-template <int kMode, bool kDup>
+template <int kMode, bool kDup, bool kLazy>
 __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
-                                                       uint32_t * __restrict__ counts)
+                                                       uint32_t * __restrict__ counts, int * __restrict__ err)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -213,6 +346,32 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                 if (kMode != kLeafUniform && (live >> (g + u) & 1u))
                     mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
             }
+            uint32_t st = 0xffu; // four states, two bits each (kBuiltDup: follow chains)
+            if (kLazy)
+            {
+                uint32_t leaf[4];
+                bool need = false;
+                st = 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u)
+                {
+                    leaf[u] = (uint32_t)(int_hash64(key[g + u]) >> shift);
+                    uint32_t v = kBuilt;
+                    if (live >> (g + u) & 1u)
+                    {
+                        note_leaf_batch(a, leaf[u]);
+                        v = load_acquire(a.leaf_state + leaf[u]);
+                    }
+                    need |= v < kBuilt;
+                    st |= v << (2 * u);
+                }
+                if (__any_sync(0xffffffffu, need))
+                {
+                    st = ensure_built_slow(a, leaf[0], leaf[1], leaf[2], leaf[3], (live >> g) & 0xfu, lane, err);
+                    if (st == kStatesTimeout)
+                        return;
+                }
+            }
             ulonglong2 cell[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
@@ -223,9 +382,9 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     continue;
                 const uint64_t h = int_hash64(key[k]);
                 if (kMode == kLeafUniform)
-                    cell[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + (h & (ucap - 1))));
+                    cell[u] = load_cell<kLazy>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + (h & (ucap - 1)));
                 else if ((mv[u].y >> 40) & 0xffu)
-                    cell[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.cells + mv[u].x + (h & ((1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)) - 1))));
+                    cell[u] = load_cell<kLazy>(a.cells + mv[u].x + (h & ((1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)) - 1)));
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
@@ -239,18 +398,18 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     {
                         const uint64_t h = int_hash64(key[k]);
                         if (kMode == kLeafUniform)
-                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, (h & (ucap - 1)) + 1, key[k]);
+                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, (h & (ucap - 1)) + 1, key[k], kLazy);
                         else
                         {
                             const uint64_t c = 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu);
-                            head = table_find_from(a.cells + mv[u].x, c, (h & (c - 1)) + 1, key[k]);
+                            head = table_find_from(a.cells + mv[u].x, c, (h & (c - 1)) + 1, key[k], kLazy);
                         }
                     }
                     if (ref_valid(head))
                     {
                         brow = build_row_of<kMode>(head, a);
-                        const bool leaf_dup = kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
-                        total += (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
+                        const bool leaf_dup = kLazy ? ((st >> (2 * u)) & 3u) == kBuiltDup : kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
+                        total += (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj, kLazy) : 1u;
                     }
                 }
                 if (live >> k & 1u)
@@ -429,9 +588,11 @@ template <int kMode, bool kDup>
 static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, uint32_t * heads, uint32_t * counts, uint64_t cap, bool lookup,
                          const char * name, uint64_t bytes)
 {
+    const bool lazy = a.leaf_state != nullptr;
+    auto lk = lazy ? k_probe_lookup<kMode, kDup, true> : k_probe_lookup<kMode, kDup, false>;
     int per_sm = 0;
     if (lookup)
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_lookup<kMode, kDup>, kPNT, 0));
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
     else
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode, kDup>, kPNT, 0));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -442,7 +603,7 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
                      (unsigned long long)n_chunks);
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
-        k_probe_lookup<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
+        lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts, ctx->d_err);
     else
         k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
     PHJ_LAUNCHED(ctx, name);
@@ -469,36 +630,57 @@ static void launch_any(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, ui
         launch_probe_mode<kLeafMeta>(ctx, a, o, heads, counts, cap, lookup, name, bytes);
 }
 
-phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+static uint64_t row_bytes_of(const Cols & c, bool with_key)
+{
+    uint64_t b = with_key ? 8 : 0;
+    for (uint32_t i = 0; i < c.n; ++i)
+        b += c.width[i];
+    return b;
+}
+
+uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, uint32_t * heads, uint32_t * counts)
 {
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
-    uint32_t * heads = s.get<uint32_t>(a.probe_rows);
-    uint32_t * counts = s.get<uint32_t>(n_chunks + 1);
-    uint64_t probe_row_bytes = 8, build_row_bytes = 0;
-    for (uint32_t c = 0; c < a.probe.n; ++c)
-        probe_row_bytes += a.probe.width[c];
-    for (uint32_t c = 0; c < a.build.n; ++c)
-        build_row_bytes += a.build.width[c];
     // algorithmic bytes: probe keys read, head array written
     launch_any(ctx, a, nullptr, heads, counts, 0, true, "probe_lookup", a.probe_rows * (8 + 4));
     scan_u32(ctx, s, counts, counts, n_chunks);
     uint32_t total = 0;
     PHJ_CUDA(cudaMemcpyAsync(&total, counts + n_chunks, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return total;
+}
+
+uint64_t probe_chunks(uint64_t probe_rows)
+{
+    return ceil_div(probe_rows, kWChunk);
+}
+
+void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_t out_base, const uint32_t * heads, const uint32_t * offs,
+                   uint64_t rows)
+{
+    OutCols o{};
+    o.keys = out->keys + out_base;
+    for (uint32_t c = 0; c < out->left.n_payloads; ++c)
+        o.left[c] = static_cast<uint8_t *>(out->lcol[c]) + out_base * payload_width(out->left.types[c]);
+    for (uint32_t c = 0; c < out->right.n_payloads; ++c)
+        o.right[c] = static_cast<uint8_t *>(out->rcol[c]) + out_base * payload_width(out->right.types[c]);
+    // algorithmic bytes: the head array, the probe key and payloads of every
+    // output row (read), the output rows (written)
+    const uint64_t pr = row_bytes_of(a.probe, true), br = row_bytes_of(a.build, false);
+    launch_any(ctx, a, &o, const_cast<uint32_t *>(heads), const_cast<uint32_t *>(offs), rows, false, "probe_project",
+               a.probe_rows * 4 + rows * pr + rows * (8 + br + (pr - 8)));
+}
+
+phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+{
+    uint32_t * heads = s.get<uint32_t>(a.probe_rows);
+    uint32_t * counts = s.get<uint32_t>(probe_chunks(a.probe_rows) + 1);
+    const uint64_t total = probe_lookup(ctx, s, a, heads, counts);
     phj_output * out = new_output(ctx, left, right, total);
     out->rows = total;
-    OutCols o{};
-    o.keys = out->keys;
-    for (uint32_t c = 0; c < out->left.n_payloads; ++c)
-        o.left[c] = out->lcol[c];
-    for (uint32_t c = 0; c < out->right.n_payloads; ++c)
-        o.right[c] = out->rcol[c];
     try
     {
-        // algorithmic bytes: the head array, the probe key and payloads of
-        // every output row (read), the output rows (written)
-        launch_any(ctx, a, &o, heads, counts, total, false, "probe_project",
-                   a.probe_rows * 4 + (uint64_t)total * probe_row_bytes + (uint64_t)total * (8 + build_row_bytes + (probe_row_bytes - 8)));
+        probe_project(ctx, a, out, 0, heads, counts, total);
     }
     catch (...)
     {

@@ -56,7 +56,7 @@ def read_output(d, b, p):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", ["c2_mini", "c3_mini", "edge"])
-@pytest.mark.parametrize("scheme", ["chj", "phj-pure"])
+@pytest.mark.parametrize("scheme", ["chj", "phj-pure", "phj"])
 def test_adapter_is_bit_exact(driver, tmp_path, name, scheme):
     b, p = cases.make(name)
     write_side(tmp_path, "build", b)

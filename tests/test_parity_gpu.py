@@ -15,12 +15,14 @@ pytestmark = pytest.mark.gpu
 GOLDEN = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "golden.json")))
 
 
-def run(ctx, scheme, b, p, bits=None, materialize=-1):
+def run(ctx, scheme, b, p, bits=None, materialize=-1, budget_mib=1):
     ctx.set_int("probe_materialize", materialize)
     tb, tp = ctx.upload(b), ctx.upload(p)
     try:
         if scheme == "chj":
             out, res = ctx.run_chj(tb, tp)
+        elif scheme == "phj":
+            out, res = ctx.run_phj_bep(tb, tp, bits, budget_mib)
         else:
             out, res = ctx.run_phj_pure(tb, tp, bits)
         jo = out.download()
@@ -42,7 +44,7 @@ def check(b, p, jo, fp=None):
 
 
 @pytest.mark.parametrize("name", cases.NAMES)
-@pytest.mark.parametrize("scheme", ["chj", "phj-pure"])
+@pytest.mark.parametrize("scheme", ["chj", "phj-pure", "phj"])
 def test_golden_cases(ctx, name, scheme):
     b, p = cases.make(name)
     jo, fp, _ = run(ctx, scheme, b, p, cases.BITS[name])
@@ -76,7 +78,7 @@ def test_no_payload_columns(ctx):
     bk = G.gen_keys(0, 5000, 1, 2)
     pk = G.gen_keys(4, 20000, 3, 2, domain=5000, match_permille=800)
     b, p = P.BlockStream([], bk, []), P.BlockStream([], pk, [])
-    for scheme in ("chj", "phj-pure"):
+    for scheme in ("chj", "phj-pure", "phj"):
         jo, fp, _ = run(ctx, scheme, b, p, [6])
         check(b, p, jo, fp)
 
@@ -97,7 +99,7 @@ def test_heavy_duplicates_single_key(ctx):
     pk = np.array([12345, 1, 12345, 7], dtype=np.uint64)
     b = P.BlockStream([P.U32], bk, G.payload_columns(8, [P.U32], 2000))
     p = P.BlockStream([P.U8], pk, G.payload_columns(9, [P.U8], 4))
-    for scheme, bits in (("chj", None), ("phj-pure", [4]), ("phj-pure", [2, 2])):
+    for scheme, bits in (("chj", None), ("phj-pure", [4]), ("phj-pure", [2, 2]), ("phj", [4]), ("phj", [2, 2])):
         jo, fp, _ = run(ctx, scheme, b, p, bits)
         check(b, p, jo, fp)
 
@@ -110,6 +112,8 @@ def test_large_leaf_uses_global_table(ctx):
     b = P.BlockStream([P.U64], bk, G.payload_columns(2, [P.U64], 40000))
     p = P.BlockStream([P.U32], G.gen_keys(4, 80000, 3, 5, domain=40000, match_permille=600), G.payload_columns(4, [P.U32], 80000))
     jo, fp, _ = run(ctx, "phj-pure", b, p, [1])
+    check(b, p, jo, fp)
+    jo, fp, _ = run(ctx, "phj", b, p, [1])
     check(b, p, jo, fp)
 
 
@@ -133,3 +137,98 @@ def test_reference_shaped_entry_points(ctx):
     r = P.runCHJ(b, p, ctx=ctx)
     assert r.build.wall_ms >= 0 and r.probe.wall_ms >= 0
     check(b, p, r.output)
+
+
+# ---- PHJ (BEP) -------------------------------------------------------------
+def bep_inputs(n_build, n_probe, seed, types_b=(P.U64,), types_p=(P.U32,), match=900):
+    bk = G.gen_keys(0, n_build, seed, seed + 1)
+    pk = G.gen_keys(4, n_probe, seed + 2, seed + 1, domain=n_build, match_permille=match)
+    return (P.BlockStream(list(types_b), bk, G.payload_columns(seed + 3, list(types_b), n_build)),
+            P.BlockStream(list(types_p), pk, G.payload_columns(seed + 4, list(types_p), n_probe)))
+
+
+@pytest.mark.parametrize("bits", [[1], [4], [3, 3], [6, 6, 6], [12], [13, 2], [4, 4, 4, 4]])
+def test_bep_radix_configs(ctx, bits):
+    b, p = cases.make("c2_mini")
+    jo, fp, res = run(ctx, "phj", b, p, bits)
+    check(b, p, jo, fp)
+    assert res.bep_budget_mib == 1
+
+
+@pytest.mark.parametrize("budget", [1, 2, 64])
+def test_bep_budget_batches_and_counters(ctx, budget):
+    # 600K probe rows of 12 bytes (7.2 MB): a 1 MiB budget gives 8 batches.
+    b, p = bep_inputs(50000, 600000, 101)
+    bits = [3, 5]
+    jo, fp, res = run(ctx, "phj", b, p, bits, budget_mib=budget)
+    check(b, p, jo, fp)
+    row_bytes = 8 + 4
+    batch_rows = min(600000, max(4096, ((budget << 20) // row_bytes) & ~255))
+    batches = -(-600000 // batch_rows)
+    assert res.bep_peak_bytes == batch_rows * row_bytes
+    assert res.bep_peak_bytes <= max(budget << 20, 4096 * row_bytes)
+    # every batch touches (nearly) every one of the 8 first-pass buckets and
+    # 256 leaves; each touched leaf is one eviction per batch
+    assert batches * 8 >= res.bep_refinements >= batches * 7
+    assert batches * 256 >= res.bep_evictions >= batches * 200
+    assert res.probe.wall_ms > 0 and res.e2e_wall_ms >= res.probe.wall_ms
+
+
+def test_bep_multi_match_edges_and_wide_payloads(ctx):
+    for name in ("c3_mini", "edge", "c4_mini", "no_match", "empty_build", "empty_probe"):
+        b, p = cases.make(name)
+        for bits in ([2], [5, 5], [3, 3, 3]):
+            jo, fp, _ = run(ctx, "phj", b, p, bits)
+            check(b, p, jo, fp)
+
+
+def test_bep_small_batches_multi_match(ctx):
+    # 16K build rows over ~4K keys, 300K probe rows with u128 payloads
+    # (24 bytes a row): 4096-row batches at the smallest budget.
+    bk, used = G.gen_multi_match_keys(16000, 131, 16)
+    pk = G.gen_keys(4, 300000, 133, 16, domain=used, match_permille=500)
+    b = P.BlockStream([P.U16, P.U128], bk, G.payload_columns(134, [P.U16, P.U128], 16000))
+    p = P.BlockStream([P.U128], pk, G.payload_columns(135, [P.U128], 300000))
+    jo, fp, res = run(ctx, "phj", b, p, [2, 4], budget_mib=1)
+    check(b, p, jo, fp)
+    assert res.bep_peak_bytes == (((1 << 20) // 24) & ~255) * 24
+
+
+def test_bep_repeated_runs_identical(ctx):
+    b, p = bep_inputs(30000, 200000, 141)
+    fps = [run(ctx, "phj", b, p, [4, 4])[1] for _ in range(3)]
+    assert fps[0] == fps[1] == fps[2]
+    assert fps[0] == run(ctx, "phj-pure", b, p, [4, 4])[1]
+
+
+def test_bep_stuck_leaf_times_out_and_context_recovers(ctx):
+    # A leaf left BUILDING (a hook that writes the state before the probe):
+    # the warps that need it give up after the wait limit, the run fails
+    # with PHJ_ERR_DEVICE_TIMEOUT, and the context runs the next join.
+    b, p = cases.make("c2_mini")
+    ctx.set_int("wait_limit_ms", 100)
+    ctx.set_int("test_stuck_leaf", 3)
+    try:
+        with pytest.raises(P.PhjError) as e:
+            run(ctx, "phj", b, p, [4])
+        assert e.value.status == P.ERR_DEVICE_TIMEOUT
+    finally:
+        ctx.set_int("test_stuck_leaf", -1)
+        ctx.set_int("wait_limit_ms", 1000)
+    jo, fp, _ = run(ctx, "phj", b, p, [4])
+    check(b, p, jo, fp)
+
+
+def test_bep_invalid_budget(ctx):
+    b, p = cases.make("c2_mini")
+    tb, tp = ctx.upload(b), ctx.upload(p)
+    with pytest.raises(P.PhjError):
+        ctx.run_phj_bep(tb, tp, [4], 0)
+    tb.free(), tp.free()
+
+
+def test_bep_reference_shaped_entry_point(ctx):
+    b, p = cases.make("c2_mini")
+    r = P.runPhjBep(b, p, [4, 4], threads=4, bep_budget_mib=1, ctx=ctx)
+    check(b, p, r.output)
+    assert r.counters["bep_budget_mib"] == 1 and r.counters["bep_evictions"] > 0
