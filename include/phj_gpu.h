@@ -128,7 +128,7 @@ typedef struct phj_bep_result {
 
 typedef struct phj_ctx phj_ctx;       /* device, stream, memory pool, timers */
 typedef struct phj_table phj_table;   /* a device-resident BlockStream */
-typedef struct phj_output phj_output; /* a device-resident JoinOutput (src/JoinOutput.h:55-70) */
+typedef struct phj_output phj_output; /* a device-resident JoinOutput (src/JoinOutput.h:64-84) */
 
 /* ---- context ---------------------------------------------------------- */
 
@@ -204,10 +204,13 @@ phj_status phj_run_phj_pure(phj_ctx *ctx, const phj_table *build, const phj_tabl
                             uint32_t n_passes, phj_output **out, phj_phj_result *result);
 
 /* runPhjBep (src/PHJBep.h:97-98, src/PHJBep.cpp:113-790): bounded probe-side
- * buffering, refinement and eviction with lazily built leaf tables inside a
- * persistent kernel.  `bep_budget_mib` is the probe-buffer budget of one
- * worker (a persistent CTA group); `workers` = number of CTA groups (0 =
- * one per SM). */
+ * buffering with lazily built leaf tables.  The probe side streams through
+ * in batches of at most `bep_budget_mib` MiB of probe rows (the reference's
+ * whole-run budget, src/PHJBep.cpp:151; at least 4096 rows a batch); each
+ * batch is scattered by the first radix pass, then probed, the first warp
+ * to need a leaf table building it (NOT_BUILT -> BUILDING -> BUILT).
+ * `workers` is the reference's `threads` and does not change the device
+ * schedule. */
 phj_status phj_run_phj_bep(phj_ctx *ctx, const phj_table *build, const phj_table *probe, const uint8_t *pass_bits,
                            uint32_t n_passes, uint64_t bep_budget_mib, uint32_t workers, phj_output **out,
                            phj_bep_result *result);
