@@ -215,6 +215,20 @@ phj_status phj_run_phj_bep(phj_ctx *ctx, const phj_table *build, const phj_table
                            uint32_t n_passes, uint64_t bep_budget_mib, uint32_t workers, phj_output **out,
                            phj_bep_result *result);
 
+/* No counterpart in the reference.  A CHJ-style join (one global table,
+ * probe, projection) that allocates no device memory, for callers that must
+ * not allocate while they join.  Its scratch is a fixed 2.5 MiB array in the
+ * library (build sides of at most 65,536 rows); the output goes into the
+ * caller's device columns (`out_keys`, `out_left[build payloads]`,
+ * `out_right[probe payloads]`) of `out_capacity` rows, in no particular
+ * order.  `*out_rows` receives the join's row count; above the capacity the
+ * call returns PHJ_ERR_CAPACITY with the first `out_capacity` rows written.
+ * The first call on a device sets up (it resolves the scratch address), so
+ * make it before capturing a stream.  Calls that overlap in time on one
+ * device race on the shared scratch: serialise them. */
+phj_status phj_run_chj_noalloc(phj_ctx *ctx, const phj_table *build, const phj_table *probe, uint64_t out_capacity,
+                               uint64_t *out_keys, void *const *out_left, void *const *out_right, uint64_t *out_rows);
+
 /* ---- output --------------------------------------------------------------- */
 
 uint64_t phj_output_rows(const phj_output *out);

@@ -120,6 +120,8 @@ def load() -> C.CDLL:
         "phj_run_phj_pure": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(P), C.POINTER(PhjResultC)]),
         "phj_run_phj_bep": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(P),
                                       C.POINTER(BepResultC)]),
+        "phj_run_chj_noalloc": (C.c_int, [P, P, P, C.c_uint64, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
+                                          C.POINTER(C.c_uint64)]),
         "phj_output_rows": (C.c_uint64, [P]),
         "phj_output_device_columns": (C.c_int, [P, C.POINTER(P), C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
         "phj_output_download": (C.c_int, [P, P, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
@@ -389,6 +391,21 @@ class Context:
         self._check(self.lib.phj_run_phj_bep(self.ptr, build.handle, probe.handle, bits, len(pass_bits), budget_mib, workers,
                                              C.byref(h), C.byref(r)))
         return Output(self, h, build.types, probe.types), r
+
+    def run_chj_noalloc(self, build: Table, probe: Table, out_capacity: int, out_keys: int, out_left: Sequence[int],
+                        out_right: Sequence[int]) -> int:
+        """The no-allocation join into caller-owned device columns (raw
+        device addresses).  Returns the join's row count; PhjError (with
+        `.rows`) when it is above `out_capacity`."""
+        rows = C.c_uint64(0)
+        lp = (C.c_void_p * MAX_PAYLOADS)(*out_left)
+        rp = (C.c_void_p * MAX_PAYLOADS)(*out_right)
+        st = self.lib.phj_run_chj_noalloc(self.ptr, build.handle, probe.handle, out_capacity, out_keys, lp, rp, C.byref(rows))
+        if st != 0:
+            err = PhjError(st, self.lib.phj_last_error(self.ptr).decode())
+            err.rows = rows.value
+            raise err
+        return rows.value
 
     # ---- measurement ----
     def kernel_times(self) -> List[dict]:
