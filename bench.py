@@ -52,7 +52,14 @@ WORKLOADS = {
            "payloads; probe 50% from the distinct build keys, u32 payload; 2 passes x 8 bits", "phj-pure",
            dict(kind=2, rows=32 * M, seed=0xD1, key_seed=0x77, types=[0, 1, 4]),
            dict(kind=4, rows=128 * M, seed=0xD2, key_seed=0x77, types=[2], domain=None, match_permille=500), [8, 8]),
+    "c4": ("PHJ (BEP) under skew 64M x 512M: unique u64 build keys with a u64 payload; probe keys Zipf(1.0) ranks through a "
+           "seeded permutation onto the build keys, u32 payload; 3 passes x 6 bits; 32 MiB probe budget per CTA group "
+           "(one group per SM); lazy per-leaf build", "phj",
+           dict(kind=0, rows=64 * M, seed=0xE1, key_seed=0x99, types=[3]),
+           dict(kind=5, rows=512 * M, seed=0xE2, key_seed=0x99, types=[2], domain=64 * M, theta=1.0), [6, 6, 6]),
 }
+# PHJ (BEP) probe budget per CTA group, MiB (--bep-budget-mib)
+BEP_BUDGET_PER_GROUP = {"c4": 32}
 
 
 def env_rank():
@@ -162,7 +169,7 @@ def make_tables(ctx, wl):
     if pspec.get("domain") is None:
         pspec["domain"] = b.gen_distinct
     p = ctx.generate(pspec["kind"], pspec["rows"], pspec["seed"], pspec["key_seed"], pspec["types"], domain=pspec["domain"],
-                     match_permille=pspec.get("match_permille", 1000))
+                     match_permille=pspec.get("match_permille", 1000), theta=pspec.get("theta", 1.0))
     return b, p
 
 
@@ -173,13 +180,23 @@ def scale_workload(name, f):
     pspec["rows"] = max(1, int(pspec["rows"] * f))
     if pspec.get("domain") and bspec["kind"] in (0, 1):
         pspec["domain"] = bspec["rows"]
+    if name in BEP_BUDGET_PER_GROUP:
+        BEP_BUDGET_PER_GROUP[name] = max(1, int(BEP_BUDGET_PER_GROUP[name] * f))
     WORKLOADS[name] = (f"{desc} [rows scaled by {f:g}]", scheme, bspec, pspec, bits)
 
 
-def run_scheme(ctx, scheme, b, p, bits):
+def run_scheme(ctx, scheme, b, p, bits, budget_mib=0):
     if scheme == "chj":
         return ctx.run_chj(b, p)
+    if scheme == "phj":
+        return ctx.run_phj_bep(b, p, bits, budget_mib)
     return ctx.run_phj_pure(b, p, bits)
+
+
+def cpu_scheme(scheme):
+    """The CPU port covers CHJ and PHJ-PURE; PHJ (BEP) is timed as PHJ-PURE,
+    the same partitioned join without the probe budget."""
+    return "phj-pure" if scheme == "phj" else scheme
 
 
 def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3):
@@ -188,11 +205,11 @@ def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3):
     probe = type(phost)(phost.types, phost.keys[:n_p], [c[:n_p] for c in phost.payloads])
     times = []
     for _ in range(reps):
-        _, ms = oracle.port_run(scheme, bhost, probe, bits, threads)
+        _, ms = oracle.port_run(cpu_scheme(scheme), bhost, probe, bits, threads)
         times.append(ms["e2e"])
     t = statistics.median(times) / 1e3
     return {"value": (len(bhost.keys) + n_p) / t, "unit": "tuples/s", "cores": threads, "kind": "port",
-            "sample": f"{scheme} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
+            "sample": f"{cpu_scheme(scheme)} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
                       f"({frac:.4g} of the probe side); median of {reps} runs, {threads} host threads; "
                       f"C++ port of the reference's scheme (oracle/cpu_port.cpp)",
             "ms_per_run": statistics.median(times)}
@@ -221,14 +238,17 @@ def reference_arm(args, rank, world, dist):
     dom = pspec.get("domain") or used
     if pspec["kind"] == 4:
         pk = G.gen_keys(4, n_p, pspec["seed"], pspec["key_seed"], domain=dom, match_permille=pspec["match_permille"])
+    elif pspec["kind"] == 5:
+        pk = G.gen_zipf_keys(n_p, pspec["seed"], pspec["key_seed"], dom, pspec.get("theta", 1.0))
     else:
         pk = G.gen_keys(pspec["kind"], n_p, pspec["seed"], pspec["key_seed"], domain=dom)
     p = P.BlockStream(pspec["types"], pk, G.payload_columns(pspec["seed"], pspec["types"], n_p))
+    cs = cpu_scheme(scheme)
     for _ in range(args.warmup):
-        oracle.port_run(scheme, b, p, bits, threads)
+        oracle.port_run(cs, b, p, bits, threads)
     times = []
     for _ in range(args.steps):
-        _, ms = oracle.port_run(scheme, b, p, bits, threads)
+        _, ms = oracle.port_run(cs, b, p, bits, threads)
         times.append(ms["e2e"])
     t = statistics.mean(times)
     value = (len(b.keys) + n_p) / (t / 1e3)
@@ -240,7 +260,7 @@ def reference_arm(args, rank, world, dist):
                    "probe_sample_of": pspec["rows"], "radix_pass_bits": bits},
         "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": threads, "kind": "port",
                          "sample": f"full build side, first {n_p} of {pspec['rows']} probe rows; C++ port of the reference's "
-                                   f"{scheme} (oracle/cpu_port.cpp) because the reference sources are not on this machine"},
+                                   f"{cs} (oracle/cpu_port.cpp) because the reference sources are not on this machine"},
         "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -253,7 +273,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--scheme", default=None, choices=["phj-pure", "chj"])
+    ap.add_argument("--scheme", default=None, choices=["phj-pure", "chj", "phj"])
+    ap.add_argument("--bep-budget-mib", type=int, default=0, help="PHJ (BEP) whole-run probe budget (default: per-group budget x SMs)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-probe-frac", type=float, default=1 / 16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -281,11 +302,12 @@ def main():
     b, p = make_tables(ctx, args.workload)
     B, Pn = b.rows, p.rows
     tuples = B + Pn
+    budget = args.bep_budget_mib or BEP_BUDGET_PER_GROUP.get(args.workload, 32) * ctx.get_int("num_sms")
 
     # -------- device-resident timing --------
     sampler = ClockSampler(local)
     for _ in range(args.warmup):
-        out, _ = run_scheme(ctx, scheme, b, p, bits)
+        out, _ = run_scheme(ctx, scheme, b, p, bits, budget)
         out.free()
     sampler.start()
     dist.barrier()
@@ -294,7 +316,7 @@ def main():
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.flush_l2()
-        out, res = run_scheme(ctx, scheme, b, p, bits)
+        out, res = run_scheme(ctx, scheme, b, p, bits, budget)
         step_ms.append(res.e2e_wall_ms)
         kernel_runs.append(ctx.kernel_times())
         out_rows = out.rows
@@ -334,7 +356,8 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u64", "data": "synthetic (seeded device generator; keys, payloads and match rate as specified)",
         "config": {"workload": desc, "scheme": scheme, "build_rows": B, "probe_rows": Pn, "radix_pass_bits": bits,
-                   "output_rows": out_rows, "l2": "inputs larger than L2 (probe side 4.3 GB) and an L2 flush between steps",
+                   "output_rows": out_rows,
+                   "l2": f"inputs larger than L2 (probe side {Pn * row_bytes(pspec['types']) / 1e9:.1f} GB) and an L2 flush between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload),
@@ -347,6 +370,12 @@ def main():
         "wall_s_timed": wall,
         "fingerprint": [str(v) for v in fp_main],
     }
+
+    if scheme == "phj":
+        line["config"]["bep_budget_mib"] = budget
+        line["bep"] = {k: getattr(res, k) for k in ("bep_evictions", "bep_refinements", "bep_peak_bytes", "bep_build_skip_retries")}
+        line["bep"]["phase_ms"] = {k: getattr(res, k).wall_ms for k in
+                                   ("build_shuffle", "build", "probe_shuffle", "probe", "eviction_overhead")}
 
     # -------- CHJ on the same inputs (extra line item) --------
     if not args.no_chj and scheme != "chj":
@@ -389,7 +418,7 @@ def main():
             dist.barrier()
             t0 = time.perf_counter()
             tb, tp = ctx.upload(pin[0]), ctx.upload(pin[1])
-            out, _ = run_scheme(ctx, scheme, tb, tp, bits)
+            out, _ = run_scheme(ctx, scheme, tb, tp, bits, budget)
             out.download((okeys, oleft, oright))
             t1 = time.perf_counter()
             out.free(), tb.free(), tp.free()

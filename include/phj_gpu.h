@@ -144,8 +144,15 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *   "probe_materialize": -1 auto (default), 0 never, 1 always -- whether the
  *        partitioned schemes write the probe side's first radix pass to
  *        memory or probe the input order directly against the leaf tables;
- *   "time_kernels": 1 (default) records CUDA events around each kernel. */
+ *   "time_kernels": 1 (default) records CUDA events around each kernel;
+ *   "wait_limit_ms": bound of a device wait on another warp's work
+ *        (PHJ/BEP leaf builds), 1..60000, default 1000;
+ *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
+ *        leaf BUILDING before the probe, so its waits run out. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);
+/* Reads an option above, or a device property: "device", "num_sms",
+ * "l2_bytes", "wait_limit_ms". */
+phj_status phj_ctx_get_int(const phj_ctx *ctx, const char *name, int64_t *value);
 
 /* ---- radix configuration: CLI.cpp:376-408 ------------------------------ */
 

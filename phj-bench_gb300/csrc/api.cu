@@ -792,6 +792,29 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
     return PHJ_OK;
 }
 
+phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * value)
+{
+    if (!ctx || !name || !value)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    if (std::strcmp(name, "probe_materialize") == 0)
+        *value = ctx->probe_materialize;
+    else if (std::strcmp(name, "time_kernels") == 0)
+        *value = ctx->time_kernels ? 1 : 0;
+    else if (std::strcmp(name, "wait_limit_ms") == 0)
+        *value = ctx->wait_limit_ms;
+    else if (std::strcmp(name, "test_stuck_leaf") == 0)
+        *value = ctx->test_stuck_leaf;
+    else if (std::strcmp(name, "device") == 0)
+        *value = ctx->device;
+    else if (std::strcmp(name, "num_sms") == 0)
+        *value = ctx->num_sms;
+    else if (std::strcmp(name, "l2_bytes") == 0)
+        *value = (int64_t)ctx->l2_bytes;
+    else
+        return PHJ_ERR_INVALID_ARGUMENT;
+    return PHJ_OK;
+}
+
 phj_status phj_resolve_radix(uint64_t partitions, uint32_t passes, const uint8_t * bits_override, uint32_t n_bits_override, uint8_t * out_bits,
                              uint32_t * out_n_passes)
 {

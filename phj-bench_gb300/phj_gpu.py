@@ -107,6 +107,7 @@ def load() -> C.CDLL:
         "phj_last_error": (C.c_char_p, [P]),
         "phj_ctx_stream": (P, [P]),
         "phj_ctx_set_int": (C.c_int, [P, C.c_char_p, C.c_int64]),
+        "phj_ctx_get_int": (C.c_int, [P, C.c_char_p, C.POINTER(C.c_int64)]),
         "phj_resolve_radix": (C.c_int, [C.c_uint64, C.c_uint32, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(C.c_uint8),
                                         C.POINTER(C.c_uint32)]),
         "phj_table_upload": (C.c_int, [P, C.POINTER(BlockStreamDesc), C.POINTER(P)]),
@@ -343,6 +344,11 @@ class Context:
 
     def set_int(self, name: str, value: int):
         self._check(self.lib.phj_ctx_set_int(self.ptr, name.encode(), int(value)))
+
+    def get_int(self, name: str) -> int:
+        v = C.c_int64()
+        self._check(self.lib.phj_ctx_get_int(self.ptr, name.encode(), C.byref(v)))
+        return v.value
 
     # ---- streams ----
     def upload(self, s: BlockStream) -> Table:
