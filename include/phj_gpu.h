@@ -126,6 +126,15 @@ typedef struct phj_bep_result {
     uint64_t bep_build_skip_retries;
 } phj_bep_result;
 
+typedef struct phj_batch_result {
+    double e2e_wall_ms;
+    uint32_t n_joins;
+    uint64_t build_rows;  /* summed over the joins */
+    uint64_t probe_rows;
+    uint64_t output_rows;
+    uint64_t peak_mem_bytes;
+} phj_batch_result;
+
 typedef struct phj_ctx phj_ctx;       /* device, stream, memory pool, timers */
 typedef struct phj_table phj_table;   /* a device-resident BlockStream */
 typedef struct phj_output phj_output; /* a device-resident JoinOutput (src/JoinOutput.h:64-84) */
@@ -221,6 +230,69 @@ phj_status phj_run_phj_pure(phj_ctx *ctx, const phj_table *build, const phj_tabl
 phj_status phj_run_phj_bep(phj_ctx *ctx, const phj_table *build, const phj_table *probe, const uint8_t *pass_bits,
                            uint32_t n_passes, uint64_t bep_budget_mib, uint32_t workers, phj_output **out,
                            phj_bep_result *result);
+
+/* Batching (no counterpart in the reference: it runs one join per call).
+ * Runs n independent joins in one set of launches (clear, build, lookup,
+ * scan, project, each over all n joins through a device work list of
+ * (join, tile) items); outs[j] receives join j's output, the same multiset
+ * of rows as a single-join entry point gives for that pair.  Meant for small
+ * and medium joins, whose single launches would not fill the device. */
+phj_status phj_batch_run(phj_ctx *ctx, uint32_t n, const phj_table *const *builds, const phj_table *const *probes,
+                         phj_output **outs, phj_batch_result *result);
+
+/* ---- serving (no counterpart in the reference) ------------------------------
+ * A request loop: requests with arrival times, admission while the summed
+ * estimated HBM footprint of the requests in flight stays within a budget,
+ * `workers` execution slots (a context and stream each) whose work overlaps
+ * on the device, and continuous batching: a free slot takes either the
+ * oldest ready request alone (run through phj_run_phj_pure with `pass_bits`)
+ * or, when that request is small, every small ready request that fits, up
+ * to `batch_max_joins`, run through phj_batch_run.  Each request's inputs
+ * are generated on the device when it starts (phj_gen_spec); its output is
+ * fingerprinted on the device and freed.  workers = 1 with batching off is
+ * the plain one-join-per-call form. */
+typedef struct phj_serve_config {
+    int device;
+    uint32_t workers;              /* execution slots, 1..64 */
+    uint64_t hbm_budget_bytes;     /* admission budget over requests in flight */
+    uint64_t batch_max_build_rows; /* requests with at most this many build rows are batched (0: never) */
+    uint32_t batch_max_joins;      /* joins per batch (<= 1: never batch) */
+    uint8_t pass_bits[8];          /* radix configuration of the joins run alone */
+    uint32_t n_passes;
+} phj_serve_config;
+
+typedef struct phj_serve_request {
+    phj_gen_spec build;
+    phj_gen_spec probe;
+    double arrival_s;              /* seconds after phj_serve_start */
+} phj_serve_request;
+
+typedef struct phj_serve_record {
+    uint64_t id;
+    double arrival_s, admit_s, start_s, done_s; /* seconds after phj_serve_start */
+    uint64_t build_rows, probe_rows, output_rows;
+    uint64_t footprint_bytes;      /* the admission estimate */
+    uint64_t fingerprint[3];       /* phj_output_fingerprint of the output */
+    uint32_t batch_size;           /* joins in the launch set that ran it (1: alone) */
+    uint32_t slot;
+    int32_t status;                /* phj_status; -1 while not done */
+} phj_serve_record;
+
+typedef struct phj_server phj_server;
+phj_status phj_serve_create(const phj_serve_config *cfg, phj_server **out);
+/* Adds a request to the trace; all requests are submitted before start. */
+phj_status phj_serve_submit(phj_server *s, const phj_serve_request *r, uint64_t *id);
+/* Starts the clock, the dispatcher and the slots. */
+phj_status phj_serve_start(phj_server *s);
+/* Waits until every request is done: PHJ_OK, PHJ_ERR_DEVICE_TIMEOUT when
+ * `timeout_s` passed first, PHJ_ERR_CUDA when a request failed. */
+phj_status phj_serve_wait(phj_server *s, double timeout_s);
+/* Copies up to `cap` records (request order); returns the request count. */
+uint32_t phj_serve_records(phj_server *s, phj_serve_record *out, uint32_t cap);
+const char *phj_serve_error(const phj_server *s);
+void phj_serve_destroy(phj_server *s);
+/* The admission estimate of a request, run alone (batched = 0) or batched. */
+uint64_t phj_serve_footprint(const phj_serve_request *r, int batched);
 
 /* No counterpart in the reference.  A CHJ-style join (one global table,
  * probe, projection) that allocates no device memory, for callers that must

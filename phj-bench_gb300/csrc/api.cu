@@ -193,36 +193,6 @@ Cols cols_from(const Cols & c, uint64_t r0)
         o.col[i] = static_cast<uint8_t *>(c.col[i]) + r0 * c.width[i];
     return o;
 }
-template <class F>
-phj_status guard(phj_ctx * ctx, F && f)
-{
-    try
-    {
-        f();
-        if (ctx)
-            ctx->last_error.clear();
-        return PHJ_OK;
-    }
-    catch (const Error & e)
-    {
-        if (ctx)
-            ctx->last_error = e.what();
-        return e.status;
-    }
-    catch (const std::bad_alloc &)
-    {
-        if (ctx)
-            ctx->last_error = "host allocation failed";
-        return PHJ_ERR_OUT_OF_MEMORY;
-    }
-    catch (const std::exception & e)
-    {
-        if (ctx)
-            ctx->last_error = e.what();
-        return PHJ_ERR_CUDA;
-    }
-}
-
 void check_schema(const phj_schema & s, const char * side)
 {
     if (s.n_payloads > PHJ_MAX_PAYLOADS)

@@ -258,4 +258,35 @@ void fingerprint(phj_ctx * ctx, const phj_output & out, uint64_t fp[3]);
 void set_partition_smem_limits(int smem_optin);
 void set_build_smem_limits(int smem_optin);
 
+// Runs f, turning exceptions into a status and the context's last error.
+template <class F>
+inline phj_status guard(phj_ctx * ctx, F && f)
+{
+    try
+    {
+        f();
+        if (ctx)
+            ctx->last_error.clear();
+        return PHJ_OK;
+    }
+    catch (const Error & e)
+    {
+        if (ctx)
+            ctx->last_error = e.what();
+        return e.status;
+    }
+    catch (const std::bad_alloc &)
+    {
+        if (ctx)
+            ctx->last_error = "host allocation failed";
+        return PHJ_ERR_OUT_OF_MEMORY;
+    }
+    catch (const std::exception & e)
+    {
+        if (ctx)
+            ctx->last_error = e.what();
+        return PHJ_ERR_CUDA;
+    }
+}
+
 } // namespace phjg

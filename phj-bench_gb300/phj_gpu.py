@@ -88,6 +88,28 @@ class KernelTime(C.Structure):
     _fields_ = [("name", C.c_char * 32), ("ms", C.c_double), ("rows", C.c_uint64), ("bytes", C.c_uint64)]
 
 
+class BatchResultC(C.Structure):
+    _fields_ = [("e2e_wall_ms", C.c_double), ("n_joins", C.c_uint32), ("build_rows", C.c_uint64), ("probe_rows", C.c_uint64),
+                ("output_rows", C.c_uint64), ("peak_mem_bytes", C.c_uint64)]
+
+
+class ServeConfig(C.Structure):
+    _fields_ = [("device", C.c_int), ("workers", C.c_uint32), ("hbm_budget_bytes", C.c_uint64),
+                ("batch_max_build_rows", C.c_uint64), ("batch_max_joins", C.c_uint32), ("pass_bits", C.c_uint8 * 8),
+                ("n_passes", C.c_uint32)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("build", GenSpec), ("probe", GenSpec), ("arrival_s", C.c_double)]
+
+
+class ServeRecord(C.Structure):
+    _fields_ = [("id", C.c_uint64), ("arrival_s", C.c_double), ("admit_s", C.c_double), ("start_s", C.c_double),
+                ("done_s", C.c_double), ("build_rows", C.c_uint64), ("probe_rows", C.c_uint64), ("output_rows", C.c_uint64),
+                ("footprint_bytes", C.c_uint64), ("fingerprint", C.c_uint64 * 3), ("batch_size", C.c_uint32), ("slot", C.c_uint32),
+                ("status", C.c_int32)]
+
+
 _lib = None
 
 
@@ -121,6 +143,15 @@ def load() -> C.CDLL:
         "phj_run_phj_pure": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(P), C.POINTER(PhjResultC)]),
         "phj_run_phj_bep": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(P),
                                       C.POINTER(BepResultC)]),
+        "phj_batch_run": (C.c_int, [P, C.c_uint32, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(BatchResultC)]),
+        "phj_serve_create": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(P)]),
+        "phj_serve_submit": (C.c_int, [P, C.POINTER(ServeRequest), C.POINTER(C.c_uint64)]),
+        "phj_serve_start": (C.c_int, [P]),
+        "phj_serve_wait": (C.c_int, [P, C.c_double]),
+        "phj_serve_records": (C.c_uint32, [P, C.POINTER(ServeRecord), C.c_uint32]),
+        "phj_serve_error": (C.c_char_p, [P]),
+        "phj_serve_destroy": (None, [P]),
+        "phj_serve_footprint": (C.c_uint64, [C.POINTER(ServeRequest), C.c_int]),
         "phj_run_chj_noalloc": (C.c_int, [P, P, P, C.c_uint64, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                           C.POINTER(C.c_uint64)]),
         "phj_output_rows": (C.c_uint64, [P]),
@@ -413,6 +444,16 @@ class Context:
             raise err
         return rows.value
 
+    def run_batch(self, builds: Sequence[Table], probes: Sequence[Table]):
+        """phj_batch_run: n joins in one set of launches; returns ([Output], result)."""
+        n = len(builds)
+        bh = (C.c_void_p * max(n, 1))(*[b.handle for b in builds])
+        ph = (C.c_void_p * max(n, 1))(*[p.handle for p in probes])
+        oh = (C.c_void_p * max(n, 1))()
+        r = BatchResultC()
+        self._check(self.lib.phj_batch_run(self.ptr, n, bh, ph, oh, C.byref(r)))
+        return [Output(self, C.c_void_p(oh[j]), builds[j].types, probes[j].types) for j in range(n)], r
+
     # ---- measurement ----
     def kernel_times(self) -> List[dict]:
         arr = (KernelTime * 256)()
@@ -490,3 +531,73 @@ def runPhjBep(build: BlockStream, probe: BlockStream, pass_bits: Sequence[int], 
                        output_rows=out.rows)
     out.free(), b.free(), p.free()
     return res
+
+
+def gen_spec(kind: int, rows: int, seed: int, key_seed: int, types: Sequence[int], domain: int = 0, match_permille: int = 1000,
+             theta: float = 1.0, block_rows: int = PIPELINE_BLOCK_ROWS) -> GenSpec:
+    sp = GenSpec()
+    sp.kind, sp.rows, sp.seed, sp.key_seed = kind, rows, seed, key_seed
+    sp.domain, sp.match_permille, sp.theta = domain, match_permille, theta
+    sp.schema = _schema_of(types)
+    sp.block_rows = block_rows
+    return sp
+
+
+class Server:
+    """The request loop (phj_serve_*): submit a trace of requests with
+    arrival offsets, start, wait, read the per-request records."""
+
+    def __init__(self, device: int = 0, workers: int = 1, hbm_budget_bytes: int = 150 << 30, batch_max_build_rows: int = 0,
+                 batch_max_joins: int = 1, pass_bits: Sequence[int] = (8, 8)):
+        self.lib = load()
+        cfg = ServeConfig()
+        cfg.device, cfg.workers, cfg.hbm_budget_bytes = device, workers, hbm_budget_bytes
+        cfg.batch_max_build_rows, cfg.batch_max_joins = batch_max_build_rows, batch_max_joins
+        for i, b in enumerate(pass_bits):
+            cfg.pass_bits[i] = b
+        cfg.n_passes = len(pass_bits)
+        self.ptr = C.c_void_p()
+        st = self.lib.phj_serve_create(C.byref(cfg), C.byref(self.ptr))
+        if st != 0:
+            raise PhjError(st, "phj_serve_create failed")
+
+    def submit(self, build: GenSpec, probe: GenSpec, arrival_s: float) -> int:
+        r = ServeRequest()
+        r.build, r.probe, r.arrival_s = build, probe, arrival_s
+        rid = C.c_uint64()
+        st = self.lib.phj_serve_submit(self.ptr, C.byref(r), C.byref(rid))
+        if st != 0:
+            raise PhjError(st, "phj_serve_submit failed")
+        return rid.value
+
+    def run(self, timeout_s: float = 600.0) -> List[dict]:
+        st = self.lib.phj_serve_start(self.ptr)
+        if st != 0:
+            raise PhjError(st, "phj_serve_start failed")
+        st = self.lib.phj_serve_wait(self.ptr, timeout_s)
+        if st != 0:
+            raise PhjError(st, self.lib.phj_serve_error(self.ptr).decode())
+        n = self.lib.phj_serve_records(self.ptr, None, 0)
+        arr = (ServeRecord * max(n, 1))()
+        self.lib.phj_serve_records(self.ptr, arr, n)
+        return [{"id": r.id, "arrival_s": r.arrival_s, "admit_s": r.admit_s, "start_s": r.start_s, "done_s": r.done_s,
+                 "build_rows": r.build_rows, "probe_rows": r.probe_rows, "output_rows": r.output_rows,
+                 "footprint_bytes": r.footprint_bytes, "fingerprint": tuple(r.fingerprint), "batch_size": r.batch_size,
+                 "slot": r.slot, "status": r.status} for r in arr[:n]]
+
+    def close(self):
+        if self.ptr:
+            self.lib.phj_serve_destroy(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def serve_footprint(build: GenSpec, probe: GenSpec, batched: bool) -> int:
+    r = ServeRequest()
+    r.build, r.probe = build, probe
+    return load().phj_serve_footprint(C.byref(r), int(batched))

@@ -70,3 +70,29 @@ def test_context_without_a_device_reports_no_device(lib):
     assert lib.phj_ctx_create(0, ctypes.byref(p)) == 6  # PHJ_ERR_NO_DEVICE
     with pytest.raises(P.PhjError):
         P.Context(0)
+
+
+def test_serve_footprint_estimate(lib):
+    # 100K unique build keys (u64 payload), 1M probe rows (u32 payload)
+    b = P.gen_spec(0, 100_000, 1, 2, [P.U64])
+    p = P.gen_spec(4, 1_000_000, 3, 2, [P.U32], domain=100_000, match_permille=500)
+    cells = 1 << 18  # bit_ceil(2 * 100K)
+    inputs = 100_000 * 16 + 1_000_000 * 12
+    table = cells * 16 + 100_000 * 8
+    out = 1_000_000 * (16 + 12 - 8)
+    assert P.serve_footprint(b, p, batched=True) == inputs + table + 1_000_000 * 4 + out
+    assert P.serve_footprint(b, p, batched=False) == inputs + table + 2 * 100_000 * 16 + 1_000_000 * 12 + 1_000_000 * 4 + out
+
+
+def test_serve_rejects_bad_config_and_needs_a_device(lib):
+    with pytest.raises(P.PhjError):
+        P.Server(workers=0)
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if not has_gpu:
+        with pytest.raises(P.PhjError) as e:
+            P.Server(workers=2)
+        assert e.value.status == 6  # PHJ_ERR_NO_DEVICE
