@@ -62,6 +62,71 @@ WORKLOADS = {
 BEP_BUDGET_PER_GROUP = {"c4": 32}
 
 
+# ---- batched / served request stream ------------------------------------
+def serve_trace(n, seed=0xC5):
+    """n join requests: build rows log-uniform in 4K..8M with unique random
+    u64 keys, probe rows = build rows x U(4,32), match rate U(0.1,1.0), 1 to 3
+    payload columns per side drawn from {u32, u64}."""
+    import phj_gpu as P
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        B = int(np.exp(rng.uniform(np.log(4096), np.log(8 * M))))
+        Pn = int(B * rng.uniform(4, 32))
+        match = int(rng.uniform(100, 1000))
+        tb = [int(t) for t in rng.choice([2, 3], size=int(rng.integers(1, 4)))]
+        tp = [int(t) for t in rng.choice([2, 3], size=int(rng.integers(1, 4)))]
+        b = P.gen_spec(0, B, seed * 7919 + 2 * i, seed * 104729 + i, tb)
+        p = P.gen_spec(4, Pn, seed * 7919 + 2 * i + 1, seed * 104729 + i, tp, domain=B, match_permille=match)
+        reqs.append((b, p, B + Pn))
+    return reqs
+
+
+def serve_once(reqs, arrivals, workers, batch_rows, batch_joins, budget):
+    import phj_gpu as P
+    srv = P.Server(workers=workers, hbm_budget_bytes=budget, batch_max_build_rows=batch_rows, batch_max_joins=batch_joins)
+    for (b, p, _), t in zip(reqs, arrivals):
+        srv.submit(b, p, float(t))
+    recs = srv.run(timeout_s=1800)
+    srv.close()
+    lat = np.array([r["done_s"] - r["arrival_s"] for r in recs])
+    span = max(r["done_s"] for r in recs) - min(r["arrival_s"] for r in recs)
+    tuples = sum(t for _, _, t in reqs)
+    return {"tuples_per_s": tuples / span, "makespan_s": span, "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3), "p999_ms": float(np.percentile(lat, 99.9) * 1e3),
+            "mean_batch": float(np.mean([r["batch_size"] for r in recs])), "requests": len(recs)}, recs
+
+
+def serving_benchmark(n_requests, workers=4, batch_rows=1 << 18, batch_joins=64, budget=150 << 30, seed=0xC5):
+    """Closed-loop capacity of the plain form (one join per call, in order)
+    and of the served form (slots + continuous batching); then Poisson
+    arrivals at 80% of the plain capacity through both, with latencies."""
+    reqs = serve_trace(n_requests, seed)
+    tuples = np.array([t for _, _, t in reqs], dtype=np.float64)
+    zero = np.zeros(len(reqs))
+    plain_cap, plain_recs = serve_once(reqs, zero, 1, 0, 1, budget)
+    served_cap, served_recs = serve_once(reqs, zero, workers, batch_rows, batch_joins, budget)
+    rate = 0.8 * plain_cap["tuples_per_s"] / tuples.mean()  # requests per second
+    rng = np.random.default_rng(seed + 1)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=len(reqs)))
+    arrivals -= arrivals[0]
+    plain_open, plain_open_recs = serve_once(reqs, arrivals, 1, 0, 1, budget)
+    served_open, served_open_recs = serve_once(reqs, arrivals, workers, batch_rows, batch_joins, budget)
+    fps = [r["fingerprint"] for r in plain_recs]
+    identical = all(fps == [r["fingerprint"] for r in rr] for rr in (served_recs, plain_open_recs, served_open_recs))
+    return {
+        "requests": n_requests, "total_tuples": float(tuples.sum()),
+        "trace": "build rows log-uniform 4K..8M (unique u64 keys), probe rows = build x U(4,32), match U(0.1,1.0), "
+                 "1-3 payload columns per side from {u32,u64}; inputs generated on the device when a request starts",
+        "plain": {"closed_loop": plain_cap, "poisson_80pct": plain_open},
+        "served": {"closed_loop": served_cap, "poisson_80pct": served_open, "slots": workers,
+                   "batch_max_build_rows": batch_rows, "batch_max_joins": batch_joins, "hbm_budget_bytes": budget},
+        "arrival_rate_req_per_s": rate,
+        "capacity_ratio_served_over_plain": served_cap["tuples_per_s"] / plain_cap["tuples_per_s"],
+        "outputs_identical_across_forms": identical,
+    }
+
+
 def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
@@ -282,11 +347,16 @@ def main():
     ap.add_argument("--no-chj", action="store_true")
     ap.add_argument("--scale", type=float, default=1.0, help="multiply both sides' rows (profiling on a smaller case)")
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="context option (phj_ctx_set_int)")
+    ap.add_argument("--serve-requests", type=int, default=2048, help="requests of the batched/served stream (0: skip it)")
+    ap.add_argument("--serve-only", action="store_true", help="run only the batched/served stream")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = Dist(world)
     if args.impl == "reference":
         reference_arm(args, rank, world, dist)
+        return
+    if args.serve_only:
+        print(json.dumps({"serving": serving_benchmark(args.serve_requests)}), flush=True)
         return
 
     import phj_gpu as P
@@ -437,6 +507,9 @@ def main():
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     b.free(), p.free()
     ctx.close()
+    # -------- batched / served request stream versus the plain form --------
+    if rank == 0 and args.serve_requests > 0:
+        line["batched_serving"] = serving_benchmark(args.serve_requests)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

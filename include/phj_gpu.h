@@ -172,6 +172,11 @@ phj_status phj_ctx_get_int(const phj_ctx *ctx, const char *name, int64_t *value)
 phj_status phj_resolve_radix(uint64_t partitions, uint32_t passes, const uint8_t *bits_override,
                              uint32_t n_bits_override, uint8_t *out_bits, uint32_t *out_n_passes);
 
+/* No counterpart in the reference (its radix bits come from the CLI): radix
+ * bits for a build side of `build_rows` rows, aiming at leaves of about 256
+ * rows (1 pass up to 11 bits, then 2 or 3 passes split evenly). */
+phj_status phj_autotune_radix(uint64_t build_rows, uint64_t probe_rows, uint8_t *out_bits, uint32_t *out_n_passes);
+
 /* ---- input streams -------------------------------------------------------- */
 
 /* Copies a host BlockStream into device memory (replaces nothing in the
@@ -258,7 +263,7 @@ typedef struct phj_serve_config {
     uint64_t batch_max_build_rows; /* requests with at most this many build rows are batched (0: never) */
     uint32_t batch_max_joins;      /* joins per batch (<= 1: never batch) */
     uint8_t pass_bits[8];          /* radix configuration of the joins run alone */
-    uint32_t n_passes;
+    uint32_t n_passes;             /* 0: phj_autotune_radix per request */
 } phj_serve_config;
 
 typedef struct phj_serve_request {

@@ -785,6 +785,24 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
     return PHJ_OK;
 }
 
+phj_status phj_autotune_radix(uint64_t build_rows, uint64_t probe_rows, uint8_t * out_bits, uint32_t * out_n_passes)
+{
+    if (!out_bits || !out_n_passes)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    (void)probe_rows;
+    // leaves of ~256 build rows: a leaf table of 512 cells (8 KiB) stays in
+    // L2 next to the probe rows that hit it; first passes of <= 11 bits keep
+    // the scatter's per-CTA digit counters in shared memory
+    uint32_t bits = 1;
+    while (bits < 24 && (build_rows >> (bits + 9)) > 0)
+        ++bits;
+    const uint32_t passes = bits <= 11 ? 1 : bits <= 22 ? 2 : 3;
+    for (uint32_t i = 0; i < passes; ++i)
+        out_bits[i] = (uint8_t)(bits / passes + (i < bits % passes ? 1 : 0));
+    *out_n_passes = passes;
+    return PHJ_OK;
+}
+
 phj_status phj_resolve_radix(uint64_t partitions, uint32_t passes, const uint8_t * bits_override, uint32_t n_bits_override, uint8_t * out_bits,
                              uint32_t * out_n_passes)
 {

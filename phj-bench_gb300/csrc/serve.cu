@@ -108,7 +108,14 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
     if (s == PHJ_OK)
     {
         if (n == 1)
-            s = phj_run_phj_pure(ctx, b[0], p[0], S.cfg.pass_bits, S.cfg.n_passes, &o[0], nullptr);
+        {
+            uint8_t bits[8];
+            uint32_t np = S.cfg.n_passes;
+            std::copy(S.cfg.pass_bits, S.cfg.pass_bits + 8, bits);
+            if (np == 0)
+                phj_autotune_radix(S.reqs[job[0]].build.rows, S.reqs[job[0]].probe.rows, bits, &np);
+            s = phj_run_phj_pure(ctx, b[0], p[0], bits, np, &o[0], nullptr);
+        }
         else
             s = phj_batch_run(ctx, (uint32_t)n, b.data(), p.data(), o.data(), nullptr);
     }
@@ -252,7 +259,7 @@ extern "C" {
 
 phj_status phj_serve_create(const phj_serve_config * cfg, phj_server ** out)
 {
-    if (!cfg || !out || cfg->workers == 0 || cfg->workers > 64 || cfg->n_passes == 0 || cfg->n_passes > 8)
+    if (!cfg || !out || cfg->workers == 0 || cfg->workers > 64 || cfg->n_passes > 8)
         return PHJ_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     phj_server * S = new phj_server();

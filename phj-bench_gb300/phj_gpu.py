@@ -143,6 +143,7 @@ def load() -> C.CDLL:
         "phj_run_phj_pure": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(P), C.POINTER(PhjResultC)]),
         "phj_run_phj_bep": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(P),
                                       C.POINTER(BepResultC)]),
+        "phj_autotune_radix": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint8), C.POINTER(C.c_uint32)]),
         "phj_batch_run": (C.c_int, [P, C.c_uint32, C.POINTER(P), C.POINTER(P), C.POINTER(P), C.POINTER(BatchResultC)]),
         "phj_serve_create": (C.c_int, [C.POINTER(ServeConfig), C.POINTER(P)]),
         "phj_serve_submit": (C.c_int, [P, C.POINTER(ServeRequest), C.POINTER(C.c_uint64)]),
@@ -548,7 +549,7 @@ class Server:
     arrival offsets, start, wait, read the per-request records."""
 
     def __init__(self, device: int = 0, workers: int = 1, hbm_budget_bytes: int = 150 << 30, batch_max_build_rows: int = 0,
-                 batch_max_joins: int = 1, pass_bits: Sequence[int] = (8, 8)):
+                 batch_max_joins: int = 1, pass_bits: Sequence[int] = ()):
         self.lib = load()
         cfg = ServeConfig()
         cfg.device, cfg.workers, cfg.hbm_budget_bytes = device, workers, hbm_budget_bytes
@@ -595,6 +596,15 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def autotune_radix(build_rows: int, probe_rows: int = 0) -> List[int]:
+    bits = (C.c_uint8 * 8)()
+    n = C.c_uint32()
+    st = load().phj_autotune_radix(build_rows, probe_rows, bits, C.byref(n))
+    if st != 0:
+        raise PhjError(st, "phj_autotune_radix failed")
+    return list(bits[: n.value])
 
 
 def serve_footprint(build: GenSpec, probe: GenSpec, batched: bool) -> int:

@@ -96,3 +96,9 @@ def test_serve_rejects_bad_config_and_needs_a_device(lib):
         with pytest.raises(P.PhjError) as e:
             P.Server(workers=2)
         assert e.value.status == 6  # PHJ_ERR_NO_DEVICE
+
+
+@pytest.mark.parametrize("rows,want", [(1, [1]), (4096, [4]), (1 << 19, [11]), (1 << 20, [6, 6]), (16 << 20, [8, 8]),
+                                       (64 << 20, [9, 9]), (1 << 31, [8, 8, 7])])
+def test_autotune_radix_leaf_target(lib, rows, want):
+    assert P.autotune_radix(rows) == want
