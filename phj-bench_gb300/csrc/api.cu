@@ -462,6 +462,9 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     LeafTables lt;
     lt.next = s.get<uint64_t>(B.rows);
     build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
+    // repeated keys: each key's rows made contiguous, so the probe expands a
+    // match as a row range
+    const bool grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
     PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
 
     // -------- PROBE SHUFFLE (src/PHJ.cpp:225-228): first pass only --------
@@ -480,7 +483,8 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
 
     // -------- PROBE with projection (src/PHJ.cpp:284-299) --------
     a.probe_rows = P.rows;
-    a.build = payload_cols(bpart);
+    a.build = payload_cols(grouped ? btmp : bpart);
+    a.grouped = grouped ? 1 : 0;
     a.meta = lt.meta;
     a.cells = lt.cells;
     a.next = lt.next;

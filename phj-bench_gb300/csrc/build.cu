@@ -96,6 +96,92 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
     }
 }
 
+// ---- grouped duplicates (PHJ-PURE with repeated build keys) ----------------
+// Position of `key` in a finished table (the key is present).
+__device__ __forceinline__ uint32_t cell_of(const Cell * tab, uint64_t cap, uint64_t h, uint64_t key)
+{
+    uint64_t pos = h & (cap - 1);
+    for (uint64_t step = 0; step < cap; ++step)
+    {
+        if (tab[pos].key == key && ref_valid(tab[pos].ref))
+            return (uint32_t)pos;
+        pos = (pos + 1) & (cap - 1);
+    }
+    return 0; // unreachable: every row's key was inserted
+}
+
+__device__ __forceinline__ void copy_row(const Cols & src, uint64_t si, const Cols & dst, uint64_t di)
+{
+    dst.keys[di] = src.keys[si];
+    for (uint32_t c = 0; c < src.n; ++c)
+        copy_elem(dst.col[c], di, src.col[c], si, src.width[c]);
+}
+
+// One CTA per leaf.  Rows of one key become contiguous in `dst`; the key's
+// cell then holds {row count, first row} (block_no, which is always 0 for
+// the single partitioned build block, carries the count), and the
+// next-chain runs last -> ... -> first.  Leaves without repeated keys are
+// copied unchanged.
+__global__ void __launch_bounds__(kBuildNT) k_group_leaf(const __grid_constant__ Cols src, const __grid_constant__ Cols dst,
+                                                         const uint32_t * __restrict__ leaf_off, const LeafMeta * __restrict__ meta,
+                                                         Cell * __restrict__ cells, uint64_t * __restrict__ next)
+{
+    extern __shared__ uint32_t gsh[]; // cnt[cap] | start[cap] | fill[cap]
+    __shared__ uint32_t warp_sums[kBuildNT / 32];
+    const uint32_t l = blockIdx.x;
+    const uint32_t r0 = leaf_off[l], r = leaf_off[l + 1] - r0;
+    if (r == 0)
+        return;
+    const LeafMeta m = meta[l];
+    if (!m.dup)
+    {
+        for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+            copy_row(src, r0 + i, dst, r0 + i);
+        return;
+    }
+    const uint32_t cap = 1u << m.log2cap;
+    Cell * tab = cells + m.table_off;
+    uint32_t * cnt = gsh;
+    uint32_t * start = gsh + cap;
+    uint32_t * fill = gsh + 2 * cap;
+    for (uint32_t i = threadIdx.x; i < cap; i += kBuildNT)
+        cnt[i] = 0;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+    {
+        const uint64_t k = src.keys[r0 + i];
+        atomicAdd(&cnt[cell_of(tab, cap, int_hash64(k), k)], 1u);
+    }
+    __syncthreads();
+    uint32_t running = 0;
+    for (uint32_t b = 0; b < cap; b += kBuildNT)
+    {
+        const uint32_t v = b + threadIdx.x < cap ? cnt[b + threadIdx.x] : 0u;
+        uint32_t tot;
+        const uint32_t ex = block_excl_scan<kBuildNT>(v, warp_sums, &tot);
+        if (b + threadIdx.x < cap)
+        {
+            start[b + threadIdx.x] = running + ex;
+            fill[b + threadIdx.x] = running + ex;
+        }
+        running += tot;
+        __syncthreads();
+    }
+    for (uint32_t c = threadIdx.x; c < cap; c += kBuildNT)
+        if (cnt[c])
+            tab[c].ref = make_ref(cnt[c], r0 + start[c]);
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+    {
+        const uint64_t k = src.keys[r0 + i];
+        const uint32_t c = cell_of(tab, cap, int_hash64(k), k);
+        const uint32_t slot = atomicAdd(&fill[c], 1u);
+        const uint64_t pos = (uint64_t)r0 + slot;
+        copy_row(src, r0 + i, dst, pos);
+        next[pos] = slot > start[c] ? make_ref(0, (uint32_t)(pos - 1)) : INVALID_REF;
+    }
+}
+
 // ---- CHJ --------------------------------------------------------------------
 
 __global__ void k_slot_hist(const uint64_t * __restrict__ keys, uint64_t n, uint32_t slot_bits, uint32_t * __restrict__ counts)
@@ -171,6 +257,23 @@ void set_build_smem_limits(int smem_optin)
 {
     const size_t need = (size_t)kSmemCellsMax * sizeof(Cell);
     PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
+    PHJ_CUDA(cudaFuncSetAttribute(k_group_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::min<size_t>((size_t)kSmemCellsMax * 12, (size_t)smem_optin - 1024)));
+}
+
+bool group_leaf_duplicates(phj_ctx * ctx, const Cols & src, const Cols & dst, const uint32_t * leaf_off, uint32_t n_leaves, const LeafTables & lt)
+{
+    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
+    if (!lt.any_dup || max_cap > kSmemCellsMax || lt.state)
+        return false;
+    uint64_t row_bytes = 8;
+    for (uint32_t c = 0; c < src.n; ++c)
+        row_bytes += src.width[c];
+    KTimer kt(ctx, "group_leaf", 0, 0);
+    k_group_leaf<<<n_leaves, kBuildNT, (size_t)max_cap * 12, ctx->stream>>>(src, dst, leaf_off, lt.meta, lt.cells, lt.next);
+    PHJ_LAUNCHED(ctx, "group_leaf");
+    (void)row_bytes;
+    return true;
 }
 
 // Lazy layout (PHJ/BEP): the directory says where each leaf's table lives;

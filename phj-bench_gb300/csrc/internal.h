@@ -211,6 +211,11 @@ struct LeafTables
 // use (PHJ/BEP).
 void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, const uint32_t * leaf_off, uint32_t n_leaves,
                        LeafTables & lt, bool lazy = false);
+// Makes the rows of each repeated key contiguous (src -> dst, one CTA per
+// leaf) so the probe expands a match as a row range instead of a chain
+// walk.  Returns false (nothing done) when no key repeats or a leaf table is
+// too large for the shared-memory counters.
+bool group_leaf_duplicates(phj_ctx * ctx, const Cols & src, const Cols & dst, const uint32_t * leaf_off, uint32_t n_leaves, const LeafTables & lt);
 // One global table of 2^slot_bits sub-tables namespaced by the top hash bits (CHJ).
 void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uint32_t slot_bits, LeafTables & lt);
 
@@ -237,6 +242,10 @@ struct ProbeArgs
     uint32_t epoch;               // this batch
     uint64_t wait_limit_ns;       // bound of a wait on a BUILDING leaf
     unsigned long long * bep_ctr; // [0] tables built, [1] waits on BUILDING, [2] leaf evictions, [3] refinements
+    // Grouped leaves (PHJ-PURE with repeated keys): a cell holds {count,
+    // first row}; the lookup records each probe row's match count here.
+    int grouped;
+    uint32_t * row_cnt;
 };
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);

@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
             for (int u = 0; u < 4; ++u)
             {
                 const int k = g + u;
-                uint32_t brow = kNoMatch;
+                uint32_t brow = kNoMatch, mcnt = 0;
                 if (ref_valid(cell[u].y))
                 {
                     uint64_t head = cell[u].y;
@@ -409,11 +409,19 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     {
                         brow = build_row_of<kMode>(head, a);
                         const bool leaf_dup = kLazy ? ((st >> (2 * u)) & 3u) == kBuiltDup : kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
-                        total += (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj, kLazy) : 1u;
+                        if (kDup && kMode != kChj && !kLazy && a.grouped)
+                            mcnt = ref_block(head) ? ref_block(head) : 1u; // grouped: {count, first row}
+                        else
+                            mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj, kLazy) : 1u;
+                        total += mcnt;
                     }
                 }
                 if (live >> k & 1u)
+                {
                     heads[row0 + (uint64_t)k * 32] = brow;
+                    if (kDup && kMode != kChj && !kLazy && a.grouped)
+                        a.row_cnt[row0 + (uint64_t)k * 32] = mcnt;
+                }
             }
         }
 #pragma unroll
@@ -556,6 +564,76 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
         }
     }
 }
+// Projection over grouped leaves: a probe row's matches are the build rows
+// [first, first + count).  Each round of 32 probe rows expands into its
+// output rows four per lane per step; a lane finds the probe row that owns
+// output j by a binary search over the warp's inclusive count prefix, so
+// every output row costs the same whatever the match counts, and the
+// stores of a step are consecutive.
+template <int kMode>
+__global__ void __launch_bounds__(kPNT) k_probe_project_grouped(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+                                                                const uint32_t * __restrict__ heads, const uint32_t * __restrict__ offs,
+                                                                uint64_t out_cap)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
+    for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
+    {
+        uint64_t base = offs[chunk];
+#pragma unroll 1
+        for (int k = 0; k < kPRPT; ++k)
+        {
+            const uint64_t row = chunk * kWChunk + (uint64_t)k * 32 + lane;
+            uint32_t first = kNoMatch, cnt = 0;
+            if (row < a.probe_rows)
+            {
+                first = __ldcs(heads + row);
+                if (first != kNoMatch)
+                    cnt = __ldcs(a.row_cnt + row);
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (uint32_t)d)
+                    incl += y;
+            }
+            const uint32_t excl = incl - cnt;
+            const uint32_t T = __shfl_sync(0xffffffffu, incl, 31);
+#pragma unroll 1
+            for (uint32_t t = 0; t < T; t += kPH * 32)
+            {
+                uint32_t brow[kPH], prow[kPH], rel[kPH], one = 0;
+#pragma unroll
+                for (int u = 0; u < kPH; ++u)
+                {
+                    const uint32_t j = t + (uint32_t)u * 32 + lane;
+                    uint32_t L = 0;
+#pragma unroll
+                    for (int b = 16; b >= 1; b >>= 1)
+                    {
+                        const uint32_t v = __shfl_sync(0xffffffffu, incl, L + b - 1);
+                        if (v <= j)
+                            L += b;
+                    }
+                    L = L > 31 ? 31 : L;
+                    const uint32_t f = __shfl_sync(0xffffffffu, first, L);
+                    const uint32_t e = __shfl_sync(0xffffffffu, excl, L);
+                    brow[u] = f + (j - e);
+                    prow[u] = (uint32_t)(chunk * kWChunk + (uint64_t)k * 32 + L);
+                    rel[u] = j;
+                    if (j < T && base + j < out_cap)
+                        one |= 1u << u;
+                }
+                project_all(pc, brow, prow, base, rel, one);
+            }
+            base += T;
+        }
+    }
+}
+
 } // namespace
 
 static ProjCols proj_cols(const ProbeArgs & a, const OutCols & o)
@@ -590,11 +668,16 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
 {
     const bool lazy = a.leaf_state != nullptr;
     auto lk = lazy ? k_probe_lookup<kMode, kDup, true> : k_probe_lookup<kMode, kDup, false>;
+    bool grouped = false;
+    if constexpr (kDup && kMode != kChj)
+        grouped = a.grouped != 0;
     int per_sm = 0;
     if (lookup)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
-    else
+    else if (!grouped)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode, kDup>, kPNT, 0));
+    else if constexpr (kDup && kMode != kChj)
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project_grouped<kMode>, kPNT, 0));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
     const unsigned grid = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>(ceil_div(std::max<uint64_t>(n_chunks, 1), kPWarps), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
@@ -605,7 +688,12 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts, ctx->d_err);
     else
-        k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
+    {
+        if (!grouped)
+            k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
+        else if constexpr (kDup && kMode != kChj)
+            k_probe_project_grouped<kMode><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
+    }
     PHJ_LAUNCHED(ctx, name);
 }
 
@@ -671,8 +759,11 @@ void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_
                a.probe_rows * 4 + rows * pr + rows * (8 + br + (pr - 8)));
 }
 
-phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, const phj_schema & left, const phj_schema & right)
 {
+    ProbeArgs a = a_in;
+    if (a.grouped && !a.row_cnt)
+        a.row_cnt = s.get<uint32_t>(std::max<uint64_t>(a.probe_rows, 1));
     uint32_t * heads = s.get<uint32_t>(a.probe_rows);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(a.probe_rows) + 1);
     const uint64_t total = probe_lookup(ctx, s, a, heads, counts);

@@ -232,3 +232,16 @@ def test_bep_reference_shaped_entry_point(ctx):
     r = P.runPhjBep(b, p, [4, 4], threads=4, bep_budget_mib=1, ctx=ctx)
     check(b, p, r.output)
     assert r.counters["bep_budget_mib"] == 1 and r.counters["bep_evictions"] > 0
+
+
+@pytest.mark.parametrize("bits", [[1], [3], [6], [4, 4]])
+def test_multi_match_grouped_and_chained_leaves(ctx, bits):
+    # [1]: leaves of ~12K rows, too large to group (chain walk); the others
+    # group each key's rows into a contiguous range.
+    bk, used = G.gen_multi_match_keys(24000, 151, 40)
+    b = P.BlockStream([P.U16, P.U128, P.U64], bk, G.payload_columns(152, [P.U16, P.U128, P.U64], 24000))
+    p = P.BlockStream([P.U32, P.U8], G.gen_keys(4, 70000, 153, 40, domain=used, match_permille=800),
+                      G.payload_columns(154, [P.U32, P.U8], 70000))
+    for materialize in (0, 1):
+        jo, fp, _ = run(ctx, "phj-pure", b, p, bits, materialize)
+        check(b, p, jo, fp)
