@@ -156,6 +156,7 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *   "time_kernels": 1 (default) records CUDA events around each kernel;
  *   "wait_limit_ms": bound of a device wait on another warp's work
  *        (PHJ/BEP leaf builds), 1..60000, default 1000;
+ *   "host_chunk_rows": probe rows per chunk of phj_run_phj_pure_host (>= 4096);
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
  *        leaf BUILDING before the probe, so its waits run out. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);
@@ -223,6 +224,20 @@ phj_status phj_run_chj(phj_ctx *ctx, const phj_table *build, const phj_table *pr
  * per-leaf tables, probe with output projection. */
 phj_status phj_run_phj_pure(phj_ctx *ctx, const phj_table *build, const phj_table *probe, const uint8_t *pass_bits,
                             uint32_t n_passes, phj_output **out, phj_phj_result *result);
+
+/* runPHJ with the BlockStreams and the JoinOutput in host memory (pinned
+ * for full speed), the form a host caller of runPHJ uses.  The build side is
+ * uploaded whole; the probe side streams through in chunks of
+ * "host_chunk_rows" rows (context option, default 16M) with the upload of
+ * the next chunk, the join of this one and the download of the previous
+ * output overlapped.  Output rows go to the host columns (`out_keys`,
+ * `out_left[build payloads]`, `out_right[probe payloads]`, `out_capacity`
+ * rows); *out_rows receives the join's row count, and above the capacity
+ * the call returns PHJ_ERR_CAPACITY with the first rows written. */
+phj_status phj_run_phj_pure_host(phj_ctx *ctx, const phj_block_stream *build, const phj_block_stream *probe,
+                                 const uint8_t *pass_bits, uint32_t n_passes, uint64_t out_capacity, uint64_t *out_keys,
+                                 void *const *out_left, void *const *out_right, uint64_t *out_rows,
+                                 phj_phj_result *result);
 
 /* runPhjBep (src/PHJBep.h:97-98, src/PHJBep.cpp:113-790): bounded probe-side
  * buffering with lazily built leaf tables.  The probe side streams through

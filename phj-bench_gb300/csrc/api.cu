@@ -3,6 +3,8 @@
 #include "internal.h"
 
 #include <cstdio>
+#include <functional>
+#include <memory>
 #include <cstring>
 #include <new>
 
@@ -652,6 +654,207 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     *out = o;
 }
 
+// PHJ-PURE with the inputs and the output in host memory.  The build side
+// is uploaded whole; the probe side streams through in chunks on three
+// streams: chunk c+1 uploads (h2d) while chunk c is partitioned by the first
+// radix pass, looked up and projected (compute) and the output of chunk c-1
+// downloads (d2h).  Two device input buffers and per-chunk outputs, each
+// reused or freed only after the copy that reads it has finished.  Output
+// rows land in the host columns chunk after chunk.
+static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const phj_block_stream & hp, const std::vector<uint32_t> & bits,
+                              uint64_t out_cap, uint64_t * out_keys, void * const * out_left, void * const * out_right, uint64_t * out_rows,
+                              phj_phj_result * res, uint64_t chunk_rows)
+{
+    if (!ctx->h2d)
+        PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+    if (!ctx->d2h)
+        PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    begin_run(ctx);
+    Scratch s(ctx);
+    cudaStream_t S = ctx->stream;
+    uint32_t total_bits = 0;
+    for (uint32_t b : bits)
+        total_bits += b;
+    const uint32_t n_leaves = 1u << total_bits;
+    const uint64_t B_rows = hb.total_rows, P_rows = hp.total_rows;
+    const uint64_t C = std::max<uint64_t>(1, std::min<uint64_t>(chunk_rows, std::max<uint64_t>(P_rows, 1)));
+    const uint64_t n_chunks = ceil_div(P_rows, C);
+    cudaEvent_t ev[4];
+    for (auto & e : ev)
+        e = take_event(ctx);
+
+    // device buffers, all allocated on the compute stream before any copy
+    phj_table * B = alloc_table(ctx, hb.schema, B_rows);
+    std::unique_ptr<phj_table, std::function<void(phj_table *)>> B_guard(B, [ctx](phj_table * t) { free_table(ctx, t); });
+    Cols in[2];
+    for (auto & c : in)
+        c = alloc_cols_like(s, hp.schema, C);
+    const Cols bpart = alloc_cols_like(s, hb.schema, B_rows);
+    const Cols btmp = alloc_cols_like(s, hb.schema, B_rows);
+    uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
+    PHJ_CUDA(cudaEventRecord(ev[0], S));
+    PHJ_CUDA(cudaStreamWaitEvent(ctx->h2d, ev[0], 0));
+
+    auto upload = [&](const Cols & dst, const phj_block_stream & src, uint64_t r0, uint64_t n) {
+        PHJ_CUDA(cudaMemcpyAsync(dst.keys, src.keys + r0, n * 8, cudaMemcpyHostToDevice, ctx->h2d));
+        for (uint32_t c = 0; c < src.schema.n_payloads; ++c)
+        {
+            const uint32_t w = payload_width(src.schema.types[c]);
+            PHJ_CUDA(cudaMemcpyAsync(dst.col[c], static_cast<const uint8_t *>(src.payloads[c]) + r0 * w, n * w, cudaMemcpyHostToDevice, ctx->h2d));
+        }
+    };
+    std::vector<cudaEvent_t> up(n_chunks), used(n_chunks), proj(n_chunks), down(n_chunks);
+    for (uint64_t c = 0; c < n_chunks; ++c)
+    {
+        up[c] = take_event(ctx);
+        used[c] = take_event(ctx);
+        proj[c] = take_event(ctx);
+        down[c] = take_event(ctx);
+    }
+    // build side, then the first two probe chunks
+    const Cols bin = cols_of(*B);
+    if (B_rows)
+        upload(bin, hb, 0, B_rows);
+    cudaEvent_t build_up = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(build_up, ctx->h2d));
+    auto enqueue_chunk = [&](uint64_t c) {
+        if (c >= 2)
+            PHJ_CUDA(cudaStreamWaitEvent(ctx->h2d, used[c - 2], 0));
+        upload(in[c & 1], hp, c * C, std::min(C, P_rows - c * C));
+        PHJ_CUDA(cudaEventRecord(up[c], ctx->h2d));
+    };
+    for (uint64_t c = 0; c < std::min<uint64_t>(2, n_chunks); ++c)
+        enqueue_chunk(c);
+
+    // -------- BUILD SHUFFLE + BUILD (src/PHJ.cpp:220-282) --------
+    PHJ_CUDA(cudaStreamWaitEvent(S, build_up, 0));
+    radix_partition(ctx, s, bin, B_rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    PHJ_CUDA(cudaEventRecord(ev[1], S));
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(B_rows);
+    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
+    const bool grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
+    PHJ_CUDA(cudaEventRecord(ev[2], S));
+
+    ProbeArgs a{};
+    a.build = payload_cols(grouped ? btmp : bpart);
+    a.grouped = grouped ? 1 : 0;
+    a.meta = lt.meta;
+    a.cells = lt.cells;
+    a.next = lt.next;
+    a.leaf_bits = total_bits;
+    a.chj = 0;
+    a.any_dup = lt.any_dup;
+    a.uniform_log2cap = lt.uniform_log2cap;
+    const bool mat = materialize_probe(ctx, lt, *B, n_leaves) && P_rows > 0;
+    const Cols ppart = mat ? alloc_cols_like(s, hp.schema, C) : Cols{};
+    const Cols ptmp = mat && bits[0] > 11 ? alloc_cols_like(s, hp.schema, C) : ppart;
+    uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
+    uint32_t * heads = s.get<uint32_t>(C);
+    uint32_t * counts = s.get<uint32_t>(probe_chunks(C) + 1);
+    if (grouped)
+        a.row_cnt = s.get<uint32_t>(C);
+
+    // -------- PROBE, chunk by chunk --------
+    std::vector<phj_output *> outs(n_chunks, nullptr);
+    uint64_t total = 0, copied = 0;
+    float t_shuffle = 0.f, t_probe = 0.f;
+    cudaEvent_t c0 = take_event(ctx), c1 = take_event(ctx), c2 = take_event(ctx);
+    try
+    {
+        for (uint64_t c = 0; c < n_chunks; ++c)
+        {
+            const uint64_t n = std::min(C, P_rows - c * C);
+            Scratch sc(ctx);
+            PHJ_CUDA(cudaStreamWaitEvent(S, up[c], 0));
+            PHJ_CUDA(cudaEventRecord(c0, S));
+            a.probe = in[c & 1];
+            if (mat)
+            {
+                radix_partition(ctx, sc, in[c & 1], n, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+                a.probe = ppart;
+                PHJ_CUDA(cudaEventRecord(used[c], S)); // the input buffer is free again
+            }
+            PHJ_CUDA(cudaEventRecord(c1, S));
+            a.probe_rows = n;
+            const uint64_t rows = probe_lookup(ctx, sc, a, heads, counts);
+            check_device_error(ctx);
+            phj_output * o = new_output(ctx, hb.schema, hp.schema, rows);
+            outs[c] = o;
+            o->rows = rows;
+            probe_project(ctx, a, o, 0, heads, counts, rows);
+            if (!mat)
+                PHJ_CUDA(cudaEventRecord(used[c], S));
+            PHJ_CUDA(cudaEventRecord(proj[c], S));
+            if (c + 2 < n_chunks)
+                enqueue_chunk(c + 2);
+            // download into the host columns at the running offset
+            PHJ_CUDA(cudaStreamWaitEvent(ctx->d2h, proj[c], 0));
+            const uint64_t keep = copied < out_cap ? std::min<uint64_t>(rows, out_cap - copied) : 0;
+            if (keep)
+            {
+                PHJ_CUDA(cudaMemcpyAsync(out_keys + copied, o->keys, keep * 8, cudaMemcpyDeviceToHost, ctx->d2h));
+                for (uint32_t k = 0; k < hb.schema.n_payloads; ++k)
+                {
+                    const uint32_t w = payload_width(hb.schema.types[k]);
+                    PHJ_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(out_left[k]) + copied * w, o->lcol[k], keep * w, cudaMemcpyDeviceToHost, ctx->d2h));
+                }
+                for (uint32_t k = 0; k < hp.schema.n_payloads; ++k)
+                {
+                    const uint32_t w = payload_width(hp.schema.types[k]);
+                    PHJ_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(out_right[k]) + copied * w, o->rcol[k], keep * w, cudaMemcpyDeviceToHost, ctx->d2h));
+                }
+            }
+            copied += keep;
+            PHJ_CUDA(cudaEventRecord(down[c], ctx->d2h));
+            total += rows;
+            // free the output two chunks back once its download is done
+            if (c >= 2 && outs[c - 2])
+            {
+                PHJ_CUDA(cudaStreamWaitEvent(S, down[c - 2], 0));
+                free_output(ctx, outs[c - 2]);
+                outs[c - 2] = nullptr;
+            }
+            PHJ_CUDA(cudaEventRecord(c2, S));
+            PHJ_CUDA(cudaEventSynchronize(c2));
+            t_shuffle += event_ms(c0, c1);
+            t_probe += event_ms(c1, c2);
+        }
+        if (n_chunks)
+            PHJ_CUDA(cudaStreamWaitEvent(S, down[n_chunks - 1], 0));
+        for (auto & o : outs)
+            if (o)
+            {
+                free_output(ctx, o);
+                o = nullptr;
+            }
+        PHJ_CUDA(cudaEventRecord(ev[3], S));
+        PHJ_CUDA(cudaEventSynchronize(ev[3]));
+    }
+    catch (...)
+    {
+        cudaStreamSynchronize(ctx->h2d);
+        cudaStreamSynchronize(ctx->d2h);
+        for (auto & o : outs)
+            free_output(ctx, o);
+        throw;
+    }
+    if (out_rows)
+        *out_rows = total;
+    if (res)
+    {
+        fill_phase(res->build_shuffle, event_ms(ev[0], ev[1]), B_rows);
+        fill_phase(res->build, event_ms(ev[1], ev[2]), B_rows);
+        fill_phase(res->probe_shuffle, t_shuffle, P_rows);
+        fill_phase(res->probe, t_probe, P_rows);
+        res->e2e_wall_ms = event_ms(ev[0], ev[3]);
+        res->peak_mem_bytes = ctx->peak_bytes;
+    }
+    if (total > out_cap)
+        throw Error(PHJ_ERR_CAPACITY, "host output holds " + std::to_string(out_cap) + " rows; the join has " + std::to_string(total) +
+                                          " (the first rows up to the capacity were written)");
+}
+
 } // namespace phjg
 
 using namespace phjg;
@@ -736,6 +939,10 @@ void phj_ctx_destroy(phj_ctx * ctx)
         cudaMemPoolDestroy(ctx->pool);
     if (ctx->stream)
         cudaStreamDestroy(ctx->stream);
+    if (ctx->h2d)
+        cudaStreamDestroy(ctx->h2d);
+    if (ctx->d2h)
+        cudaStreamDestroy(ctx->d2h);
     delete ctx;
 }
 
@@ -759,6 +966,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->time_kernels = value != 0;
     else if (std::strcmp(name, "wait_limit_ms") == 0 && value >= 1 && value <= 60000)
         ctx->wait_limit_ms = value;
+    else if (std::strcmp(name, "host_chunk_rows") == 0 && value >= 4096)
+        ctx->host_chunk_rows = value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
     else
@@ -776,6 +985,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->time_kernels ? 1 : 0;
     else if (std::strcmp(name, "wait_limit_ms") == 0)
         *value = ctx->wait_limit_ms;
+    else if (std::strcmp(name, "host_chunk_rows") == 0)
+        *value = ctx->host_chunk_rows;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
     else if (std::strcmp(name, "device") == 0)
@@ -1020,6 +1231,36 @@ phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_tab
         if (bep_budget_mib == 0 || bep_budget_mib > (1ull << 30))
             throw Error(PHJ_ERR_INVALID_ARGUMENT, "bep_budget_mib must be in [1, 2^30]");
         run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
+    });
+}
+
+phj_status phj_run_phj_pure_host(phj_ctx * ctx, const phj_block_stream * build, const phj_block_stream * probe, const uint8_t * pass_bits,
+                                 uint32_t n_passes, uint64_t out_capacity, uint64_t * out_keys, void * const * out_left, void * const * out_right,
+                                 uint64_t * out_rows, phj_phj_result * result)
+{
+    if (!ctx || !build || !probe)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    if (out_rows)
+        *out_rows = 0;
+    return guard(ctx, [&] {
+        const std::vector<uint32_t> bits = check_bits(pass_bits, n_passes);
+        check_schema(build->schema, "build stream");
+        check_schema(probe->schema, "probe stream");
+        if (build->location != PHJ_HOST || probe->location != PHJ_HOST)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "phj_run_phj_pure_host takes host streams");
+        if (build->total_rows >= (1ull << 31) || probe->total_rows >= (1ull << 32))
+            throw Error(PHJ_ERR_UNSUPPORTED, "device schemes support < 2^31 build rows and < 2^32 probe rows");
+        if ((build->total_rows && !build->keys) || (probe->total_rows && !probe->keys))
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "null key column");
+        if (out_capacity && !out_keys)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "null output key column");
+        for (uint32_t c = 0; c < build->schema.n_payloads; ++c)
+            if ((build->total_rows && !build->payloads[c]) || (out_capacity && (!out_left || !out_left[c])))
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "null build payload column");
+        for (uint32_t c = 0; c < probe->schema.n_payloads; ++c)
+            if ((probe->total_rows && !probe->payloads[c]) || (out_capacity && (!out_right || !out_right[c])))
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "null probe payload column");
+        run_phj_pure_host(ctx, *build, *probe, bits, out_capacity, out_keys, out_left, out_right, out_rows, result, (uint64_t)ctx->host_chunk_rows);
     });
 }
 

@@ -70,6 +70,7 @@ struct phj_ctx
     size_t smem_optin = 0;
     size_t l2_bytes = 0;
     cudaStream_t stream = nullptr;
+    cudaStream_t h2d = nullptr, d2h = nullptr; // copy streams of the host-buffer entry points (made on first use)
     cudaMemPool_t pool = nullptr;
     std::string last_error;
     uint64_t launches = 0;
@@ -87,6 +88,7 @@ struct phj_ctx
     // Options (phj_ctx_set_int).
     int probe_materialize = -1; // -1 auto, 0 never, 1 always
     int64_t wait_limit_ms = 1000; // bound of a device wait on another warp's work
+    int64_t host_chunk_rows = 16ll << 20; // probe rows per chunk of the host-buffer entry points
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
 };
 

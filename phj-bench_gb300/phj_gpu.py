@@ -141,6 +141,9 @@ def load() -> C.CDLL:
         "phj_table_free": (None, [P, P]),
         "phj_run_chj": (C.c_int, [P, P, P, C.POINTER(P), C.POINTER(ChjResultC)]),
         "phj_run_phj_pure": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(P), C.POINTER(PhjResultC)]),
+        "phj_run_phj_pure_host": (C.c_int, [P, C.POINTER(BlockStreamDesc), C.POINTER(BlockStreamDesc), C.POINTER(C.c_uint8), C.c_uint32,
+                                            C.c_uint64, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                            C.POINTER(PhjResultC)]),
         "phj_run_phj_bep": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(P),
                                       C.POINTER(BepResultC)]),
         "phj_autotune_radix": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint8), C.POINTER(C.c_uint32)]),
@@ -383,6 +386,33 @@ class Context:
         return v.value
 
     # ---- streams ----
+    @staticmethod
+    def _desc(s: BlockStream) -> "BlockStreamDesc":
+        d = BlockStreamDesc()
+        d.schema = s.schema()
+        d.total_rows = s.total_rows
+        d.n_blocks = len(s.block_rows)
+        d.block_rows = s.block_rows.ctypes.data_as(C.POINTER(C.c_uint32)) if len(s.block_rows) else None
+        d.keys = s.keys.ctypes.data if s.total_rows else None
+        for i, p in enumerate(s.payloads):
+            d.payloads[i] = p.ctypes.data if s.total_rows else None
+        d.location = 0
+        return d
+
+    def run_phj_pure_host(self, build: BlockStream, probe: BlockStream, pass_bits: Sequence[int], out_keys: np.ndarray,
+                          out_left: Sequence[np.ndarray], out_right: Sequence[np.ndarray]):
+        """phj_run_phj_pure_host: host inputs, host output columns (pinned
+        for full speed).  Returns (output rows, PhjResultC)."""
+        db, dp = self._desc(build), self._desc(probe)
+        bits = (C.c_uint8 * max(1, len(pass_bits)))(*pass_bits)
+        lp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_left])
+        rp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_right])
+        rows = C.c_uint64()
+        r = PhjResultC()
+        self._check(self.lib.phj_run_phj_pure_host(self.ptr, C.byref(db), C.byref(dp), bits, len(pass_bits), len(out_keys),
+                                                   out_keys.ctypes.data, lp, rp, C.byref(rows), C.byref(r)))
+        return rows.value, r
+
     def upload(self, s: BlockStream) -> Table:
         d = BlockStreamDesc()
         d.schema = s.schema()

@@ -245,3 +245,47 @@ def test_multi_match_grouped_and_chained_leaves(ctx, bits):
     for materialize in (0, 1):
         jo, fp, _ = run(ctx, "phj-pure", b, p, bits, materialize)
         check(b, p, jo, fp)
+
+
+# ---- PHJ-PURE with host buffers (streamed probe chunks) ----------------------
+def host_out(ctx, b, p, cap, pinned=True):
+    def alloc(shape, dt):
+        return ctx.pinned(shape, dt) if pinned else np.empty(shape, dtype=dt)
+    keys = alloc((cap,), np.uint64)
+    left = [alloc((cap, 2), np.uint64) if t == P.U128 else alloc((cap,), P.TYPE_DTYPE[t]) for t in b.types]
+    right = [alloc((cap, 2), np.uint64) if t == P.U128 else alloc((cap,), P.TYPE_DTYPE[t]) for t in p.types]
+    return keys, left, right
+
+
+@pytest.mark.parametrize("name", ["c2_mini", "c3_mini", "edge", "empty_probe", "empty_build", "no_match"])
+@pytest.mark.parametrize("chunk", [4096, 1 << 24])
+def test_host_buffer_phj_pure(ctx, name, chunk):
+    b, p = cases.make(name)
+    expected = O.join_rows(b, p)
+    ctx.set_int("host_chunk_rows", chunk)
+    try:
+        keys, left, right = host_out(ctx, b, p, len(expected) + 5, pinned=(chunk == 4096))
+        rows, res = ctx.run_phj_pure_host(b, p, cases.BITS[name], keys, left, right)
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
+    assert rows == len(expected)
+    jo = P.JoinOutput(b.types, p.types, keys[:rows], [c[:rows] for c in left], [c[:rows] for c in right])
+    assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
+    assert res.e2e_wall_ms > 0
+
+
+def test_host_buffer_short_capacity(ctx):
+    b, p = cases.make("c2_mini")
+    expected = O.join_rows(b, p)
+    ctx.set_int("host_chunk_rows", 8192)
+    try:
+        keys, left, right = host_out(ctx, b, p, 1000)
+        with pytest.raises(P.PhjError) as e:
+            ctx.run_phj_pure_host(b, p, [4, 4], keys, left, right)
+        assert e.value.status == 7
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
+    # the context keeps working
+    keys, left, right = host_out(ctx, b, p, len(expected))
+    rows, _ = ctx.run_phj_pure_host(b, p, [4, 4], keys, left, right)
+    assert rows == len(expected)
