@@ -968,6 +968,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->wait_limit_ms = value;
     else if (std::strcmp(name, "host_chunk_rows") == 0 && value >= 4096)
         ctx->host_chunk_rows = value;
+    else if (std::strcmp(name, "table_cap_pct") == 0 && value >= 110 && value <= 800)
+        ctx->table_cap_pct = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
     else

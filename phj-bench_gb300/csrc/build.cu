@@ -21,13 +21,24 @@ namespace
 constexpr int kBuildNT = 256;
 constexpr uint32_t kSmemCellsMax = 8192; // 128 KiB of cells per CTA
 
-__global__ void k_leaf_caps(const uint32_t * __restrict__ leaf_off, uint32_t n_leaves, uint32_t * __restrict__ caps, uint32_t * __restrict__ max_rows)
+// Cells of a table for r rows: the power of two at or above r * pct / 100
+// (pct 200: load <= 1/2, the reference's JoinHashTable::reserve), and above r.
+__host__ __device__ __forceinline__ uint64_t table_cells(uint64_t r, uint32_t pct)
+{
+    if (!r)
+        return 0;
+    const uint64_t want = (r * pct + 99) / 100;
+    return bit_ceil64(want > r ? want : r + 1);
+}
+
+__global__ void k_leaf_caps(const uint32_t * __restrict__ leaf_off, uint32_t n_leaves, uint32_t pct, uint32_t * __restrict__ caps,
+                            uint32_t * __restrict__ max_rows)
 {
     const uint32_t l = blockIdx.x * blockDim.x + threadIdx.x;
     if (l >= n_leaves)
         return;
     const uint32_t r = leaf_off[l + 1] - leaf_off[l];
-    caps[l] = r ? (uint32_t)bit_ceil64(2ull * r) : 0u;
+    caps[l] = (uint32_t)table_cells(r, pct);
     if (r)
         atomicMax(max_rows, r);
 }
@@ -263,7 +274,7 @@ void set_build_smem_limits(int smem_optin)
 
 bool group_leaf_duplicates(phj_ctx * ctx, const Cols & src, const Cols & dst, const uint32_t * leaf_off, uint32_t n_leaves, const LeafTables & lt)
 {
-    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
+    const uint64_t max_cap = lt.max_rows ? table_cells(lt.max_rows, ctx->table_cap_pct) : 1;
     if (!lt.any_dup || max_cap > kSmemCellsMax || lt.state)
         return false;
     uint64_t row_bytes = 8;
@@ -298,7 +309,7 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     uint32_t * table_off = s.get<uint32_t>(n_leaves + 1);
     uint32_t * small = s.get<uint32_t>(4); // [0] max rows, [1] any dup
     PHJ_CUDA(cudaMemsetAsync(small, 0, 4 * sizeof(uint32_t), ctx->stream));
-    k_leaf_caps<<<(unsigned)ceil_div(n_leaves, 256), 256, 0, ctx->stream>>>(leaf_off, n_leaves, caps, small);
+    k_leaf_caps<<<(unsigned)ceil_div(n_leaves, 256), 256, 0, ctx->stream>>>(leaf_off, n_leaves, ctx->table_cap_pct, caps, small);
     PHJ_LAUNCHED(ctx, "leaf_caps");
     scan_u32(ctx, s, caps, table_off, n_leaves);
     uint32_t host[2] = {0, 0};
@@ -306,7 +317,7 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     PHJ_CUDA(cudaMemcpyAsync(&host[1], table_off + n_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
     lt.max_rows = host[0];
-    const uint64_t max_cap = lt.max_rows ? bit_ceil64(2ull * lt.max_rows) : 1;
+    const uint64_t max_cap = lt.max_rows ? table_cells(lt.max_rows, ctx->table_cap_pct) : 1;
     // Uniform capacity (the largest leaf's) lets the probe compute a table's
     // address from the leaf id alone; it is used unless it costs more than
     // 1.5x the cells of per-leaf sizing.
@@ -359,7 +370,7 @@ void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uin
     // reuse k_leaf_caps on a prefix of the counts.
     uint32_t * cnt_off = s.get<uint32_t>(n_slots + 1);
     scan_u32(ctx, s, counts, cnt_off, n_slots);
-    k_leaf_caps<<<(unsigned)ceil_div(n_slots, 256), 256, 0, ctx->stream>>>(cnt_off, n_slots, caps, max_rows);
+    k_leaf_caps<<<(unsigned)ceil_div(n_slots, 256), 256, 0, ctx->stream>>>(cnt_off, n_slots, 200u, caps, max_rows);
     PHJ_LAUNCHED(ctx, "chj_caps");
     scan_u32(ctx, s, caps, table_off, n_slots);
     uint32_t total = 0;

@@ -89,6 +89,7 @@ struct phj_ctx
     int probe_materialize = -1; // -1 auto, 0 never, 1 always
     int64_t wait_limit_ms = 1000; // bound of a device wait on another warp's work
     int64_t host_chunk_rows = 16ll << 20; // probe rows per chunk of the host-buffer entry points
+    uint32_t table_cap_pct = 200; // leaf table cells >= rows * pct / 100 (power of two)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
 };
 
