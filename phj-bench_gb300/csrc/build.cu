@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
 // Position of `key` in a finished table (the key is present).
 __device__ __forceinline__ uint32_t cell_of(const Cell * tab, uint64_t cap, uint64_t h, uint64_t key)
 {
-    uint64_t pos = h & (cap - 1);
+    uint64_t pos = probe_start(h, cap);
     for (uint64_t step = 0; step < cap; ++step)
     {
         if (tab[pos].key == key && ref_valid(tab[pos].ref))
@@ -317,7 +317,8 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     PHJ_CUDA(cudaMemcpyAsync(&host[1], table_off + n_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
     lt.max_rows = host[0];
-    const uint64_t max_cap = lt.max_rows ? table_cells(lt.max_rows, ctx->table_cap_pct) : 1;
+    // at least one aligned cell pair: the probe's first load reads two cells
+    const uint64_t max_cap = lt.max_rows ? table_cells(lt.max_rows, ctx->table_cap_pct) : 2;
     // Uniform capacity (the largest leaf's) lets the probe compute a table's
     // address from the leaf id alone; it is used unless it costs more than
     // 1.5x the cells of per-leaf sizing.

@@ -76,8 +76,18 @@ __device__ __forceinline__ Cell cas_cell_shared(Cell *p, Cell cmp, Cell val)
     return old;
 }
 
+// Linear probing starts at the even cell of the hash's pair, so that the
+// first two probe positions share one aligned 32-byte sector and arrive
+// with one load.
+__host__ __device__ __forceinline__ uint64_t probe_start(uint64_t hash, uint64_t cap)
+{
+    return hash & (cap - 1) & ~1ull;
+}
+
 // Insert (key, ref) into an open-addressing table of `cap` (power of two)
-// cells with linear probing from `hash & (cap-1)` (src/HashTable.h:84-109).
+// cells with linear probing from probe_start(hash) (src/HashTable.h:84-109
+// probes from hash & (cap-1); starting at the pair's even cell changes no
+// lookup result).
 // Returns the previous head ref for `key` (INVALID_REF when new), which the
 // caller threads into the next-chain.  Concurrent inserters are safe: an
 // empty cell is claimed with one 128-bit CAS; a cell that already holds the
@@ -88,7 +98,7 @@ template <bool kShared>
 __device__ __forceinline__ uint64_t table_insert(Cell *cells, uint64_t cap, uint64_t hash, uint64_t key, uint64_t ref)
 {
     const uint64_t mask = cap - 1;
-    uint64_t pos = hash & mask;
+    uint64_t pos = probe_start(hash, cap);
     const Cell empty{0ull, INVALID_REF};
     const Cell mine{key, ref};
     for (uint64_t step = 0; step < cap; ++step)
@@ -110,7 +120,7 @@ __device__ __forceinline__ uint64_t table_find(const Cell *cells, uint64_t cap, 
     if (cap == 0)
         return INVALID_REF;
     const uint64_t mask = cap - 1;
-    uint64_t pos = hash & mask;
+    uint64_t pos = probe_start(hash, cap);
     for (uint64_t step = 0; step < cap; ++step)
     {
         const ulonglong2 c = __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
@@ -121,6 +131,24 @@ __device__ __forceinline__ uint64_t table_find(const Cell *cells, uint64_t cap, 
         pos = (pos + 1) & mask;
     }
     return INVALID_REF;
+}
+
+// The two cells of an aligned pair with one 256-bit load (cap >= 2): through
+// the read-only path, or through L2 when the table may still be written
+// (coherent).
+struct CellPair
+{
+    ulonglong2 a, b;
+};
+template <bool kCoherent>
+__device__ __forceinline__ CellPair load_pair(const Cell *p)
+{
+    CellPair r;
+    if (kCoherent)
+        asm volatile("ld.global.cg.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(r.a.x), "=l"(r.a.y), "=l"(r.b.x), "=l"(r.b.y) : "l"(p) : "memory");
+    else
+        asm("ld.global.nc.v4.u64 {%0, %1, %2, %3}, [%4];" : "=l"(r.a.x), "=l"(r.a.y), "=l"(r.b.x), "=l"(r.b.y) : "l"(p));
+    return r;
 }
 
 // ---------------------------------------------------------------------------

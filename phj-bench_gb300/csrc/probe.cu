@@ -316,6 +316,10 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
     const uint32_t shift = 64u - a.leaf_bits;
     const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
     const uint64_t ucap = 1ull << ulog;
+    __shared__ uint64_t q_key[kLazy ? 1 : kPWarps * kWChunk];
+    __shared__ uint16_t q_row[kLazy ? 1 : kPWarps * kWChunk];
+    uint64_t * qkey = q_key + (kLazy ? 0 : (threadIdx.x >> 5) * kWChunk);
+    uint16_t * qrow = q_row + (kLazy ? 0 : (threadIdx.x >> 5) * kWChunk);
     for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
     {
         const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
@@ -333,6 +337,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
             }
         }
         uint32_t total = 0;
+        uint32_t qn = 0; // rows in the warp's queue
         // four directory loads (per-leaf tables), four first-cell loads,
         // then the comparisons: four table requests in flight per lane
 #pragma unroll
@@ -372,39 +377,70 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                         return;
                 }
             }
-            ulonglong2 cell[4];
+            CellPair cell[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
                 const int k = g + u;
-                cell[u] = make_ulonglong2(0ull, INVALID_REF);
+                cell[u].a = make_ulonglong2(0ull, INVALID_REF);
+                cell[u].b = cell[u].a;
                 if (!(live >> k & 1u))
                     continue;
                 const uint64_t h = int_hash64(key[k]);
                 if (kMode == kLeafUniform)
-                    cell[u] = load_cell<kLazy>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + (h & (ucap - 1)));
+                    cell[u] = load_pair<kLazy>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
                 else if ((mv[u].y >> 40) & 0xffu)
-                    cell[u] = load_cell<kLazy>(a.cells + mv[u].x + (h & ((1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)) - 1)));
+                    cell[u] = load_pair<kLazy>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
                 const int k = g + u;
                 uint32_t brow = kNoMatch, mcnt = 0;
-                if (ref_valid(cell[u].y))
+                // the pair's two cells are the first two probe positions
+                uint64_t head = INVALID_REF;
+                bool more = false;
+                if (ref_valid(cell[u].a.y))
                 {
-                    uint64_t head = cell[u].y;
-                    if (cell[u].x != key[k])
+                    if (cell[u].a.x == key[k])
+                        head = cell[u].a.y;
+                    else if (ref_valid(cell[u].b.y))
+                    {
+                        if (cell[u].b.x == key[k])
+                            head = cell[u].b.y;
+                        else
+                            more = true;
+                    }
+                }
+                if constexpr (kLazy)
+                {
+                    if (more)
                     {
                         const uint64_t h = int_hash64(key[k]);
                         if (kMode == kLeafUniform)
-                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, (h & (ucap - 1)) + 1, key[k], kLazy);
+                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, key[k], kLazy);
                         else
                         {
                             const uint64_t c = 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu);
-                            head = table_find_from(a.cells + mv[u].x, c, (h & (c - 1)) + 1, key[k], kLazy);
+                            head = table_find_from(a.cells + mv[u].x, c, probe_start(h, c) + 2, key[k], kLazy);
                         }
                     }
+                }
+                else
+                {
+                    // rows whose key lies past the cell pair wait in the
+                    // warp's queue and are probed together after the chunk
+                    const uint32_t m = __ballot_sync(0xffffffffu, more);
+                    if (more)
+                    {
+                        const uint32_t slot = qn + __popc(m & ((1u << lane) - 1u));
+                        qkey[slot] = key[k];
+                        qrow[slot] = (uint16_t)(k * 32 + lane);
+                    }
+                    qn += __popc(m);
+                }
+                if (!more || kLazy)
+                {
                     if (ref_valid(head))
                     {
                         brow = build_row_of<kMode>(head, a);
@@ -416,13 +452,48 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                         total += mcnt;
                     }
                 }
-                if (live >> k & 1u)
+                if ((live >> k & 1u) && (!more || kLazy))
                 {
                     heads[row0 + (uint64_t)k * 32] = brow;
                     if (kDup && kMode != kChj && !kLazy && a.grouped)
                         a.row_cnt[row0 + (uint64_t)k * 32] = mcnt;
                 }
             }
+        }
+        if constexpr (!kLazy)
+        {
+            __syncwarp();
+            for (uint32_t j = lane; j < qn; j += 32)
+            {
+                const uint64_t qk = qkey[j];
+                const uint64_t row = chunk * kWChunk + qrow[j];
+                const uint64_t h = int_hash64(qk);
+                uint64_t head;
+                bool leaf_dup = true;
+                if (kMode == kLeafUniform)
+                    head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, qk);
+                else
+                {
+                    const ulonglong2 m = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(h >> shift)));
+                    const uint64_t c = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
+                    head = table_find_from(a.cells + m.x, c, probe_start(h, c) + 2, qk);
+                    leaf_dup = ((m.y >> 48) & 1u) != 0;
+                }
+                uint32_t brow = kNoMatch, mcnt = 0;
+                if (ref_valid(head))
+                {
+                    brow = build_row_of<kMode>(head, a);
+                    if (kDup && kMode != kChj && a.grouped)
+                        mcnt = ref_block(head) ? ref_block(head) : 1u;
+                    else
+                        mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
+                    total += mcnt;
+                }
+                heads[row] = brow;
+                if (kDup && kMode != kChj && a.grouped)
+                    a.row_cnt[row] = mcnt;
+            }
+            __syncwarp();
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
@@ -684,6 +755,9 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     if (std::getenv("PHJ_DEBUG"))
         std::fprintf(stderr, "[phj] %s: mode %d dup %d grid %u x %d threads, %d CTAs/SM, chunks %llu\n", name, kMode, (int)kDup, grid, kPNT, per_sm,
                      (unsigned long long)n_chunks);
+    // the first probe load reads an aligned pair of cells
+    if ((kMode == kLeafUniform && a.uniform_log2cap < 1) || (reinterpret_cast<uintptr_t>(a.cells) & 31) != 0)
+        throw Error(PHJ_ERR_CUDA, "internal: leaf tables need aligned pairs of cells");
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts, ctx->d_err);
