@@ -513,10 +513,10 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
 // PHJ (BEP).  The build side is shuffled to full leaf depth and its leaf
 // tables are planned but left NOT_BUILT; the probe side streams through in
 // batches of at most the byte budget.  Each batch is scattered by the first
-// radix pass (probe shuffle), then probed against the leaf tables, the first
-// warp to reach a leaf building its table.  A batch's probe drains every
-// leaf it touched, which is the device form of the reference's eviction
-// (src/PHJBep.cpp:113-790).
+// radix pass (probe shuffle), the leaves it touches and that are still
+// NOT_BUILT are built from a device work queue, then the batch is probed.
+// A batch's probe drains every leaf it touched, which is the device form of
+// the reference's eviction (src/PHJBep.cpp:113-790).
 static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P, const std::vector<uint32_t> & bits, uint64_t budget_mib,
                         phj_output ** out, phj_bep_result * res)
 {
@@ -526,7 +526,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     for (uint32_t b : bits)
         total_bits += b;
     const uint32_t n_leaves = 1u << total_bits;
-    cudaEvent_t ev[3], eb[3];
+    cudaEvent_t ev[3], eb[5];
     for (auto & e : ev)
         e = take_event(ctx);
     for (auto & e : eb)
@@ -554,9 +554,9 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
 
     unsigned long long * ctr = s.get<unsigned long long>(4);
-    uint32_t * epoch = s.get<uint32_t>(n_leaves);
+    uint32_t * touched = s.get<uint32_t>((n_leaves + 31) / 32);
     PHJ_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(epoch, 0, (size_t)n_leaves * sizeof(uint32_t), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(touched, 0, (size_t)((n_leaves + 31) / 32) * 4, ctx->stream));
 
     ProbeArgs a{};
     a.build = payload_cols(bpart);
@@ -565,14 +565,26 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     a.next = lt.next;
     a.leaf_bits = total_bits;
     a.chj = 0;
-    a.any_dup = 1;
+    a.any_dup = 0;
     a.uniform_log2cap = lt.uniform_log2cap;
-    a.leaf_state = lt.state;
-    a.leaf_off = leaf_off;
-    a.build_keys = bpart.keys;
-    a.leaf_epoch = epoch;
-    a.wait_limit_ns = (uint64_t)ctx->wait_limit_ms * 1000000ull;
-    a.bep_ctr = ctr;
+    BepLeaves bl{};
+    bl.state = lt.state;
+    bl.touched = touched;
+    bl.leaf_off = leaf_off;
+    bl.build_keys = bpart.keys;
+    bl.meta = lt.meta;
+    bl.cells = lt.cells;
+    bl.next = lt.next;
+    bl.leaf_bits = total_bits;
+    bl.n_leaves = n_leaves;
+    bl.smem_cells = (uint32_t)std::min<uint64_t>(lt.uniform_log2cap >= 0 ? (1ull << lt.uniform_log2cap) : bit_ceil64(2ull * std::max<uint32_t>(lt.max_rows, 1)),
+                                                 8192);
+    bl.wait_limit_ns = (uint64_t)ctx->wait_limit_ms * 1000000ull;
+    bl.ctr = ctr;
+    bl.queue = s.get<uint32_t>(n_leaves);
+    bl.queue_len = s.get<uint32_t>(2);
+    bl.any_dup = s.get<int>(1);
+    PHJ_CUDA(cudaMemsetAsync(bl.any_dup, 0, sizeof(int), ctx->stream));
 
     // -------- PROBE: budget-sized batches --------
     const uint64_t row_bytes = 8 + schema_bytes(P.schema);
@@ -587,7 +599,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     uint32_t * counts = s.get<uint32_t>(probe_chunks(batch_rows) + 1);
     phj_output * o = nullptr;
     uint64_t total = 0, peak_rows = 0;
-    float t_shuffle = 0.f, t_probe = 0.f;
+    float t_shuffle = 0.f, t_probe = 0.f, t_lazy = 0.f;
     try
     {
         uint32_t e = 1;
@@ -603,9 +615,12 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             PHJ_CUDA(cudaEventRecord(eb[1], ctx->stream));
             a.probe = ppart;
             a.probe_rows = n_b;
-            a.epoch = e;
-            const uint64_t rows = probe_lookup(ctx, sb, a, heads, counts);
+            // lazy build of the leaves this batch touches
+            PHJ_CUDA(cudaEventRecord(eb[3], ctx->stream));
+            a.any_dup = bep_build_touched(ctx, bl, ppart.keys, n_b) ? 1 : 0;
             check_device_error(ctx);
+            PHJ_CUDA(cudaEventRecord(eb[4], ctx->stream));
+            const uint64_t rows = probe_lookup(ctx, sb, a, heads, counts);
             if (!o)
             {
                 // first batch: extrapolate the output size over the stream
@@ -619,7 +634,8 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             PHJ_CUDA(cudaEventRecord(eb[2], ctx->stream));
             PHJ_CUDA(cudaEventSynchronize(eb[2]));
             t_shuffle += event_ms(eb[0], eb[1]);
-            t_probe += event_ms(eb[1], eb[2]);
+            t_lazy += event_ms(eb[3], eb[4]);
+            t_probe += event_ms(eb[4], eb[2]);
         }
         if (!o)
             o = new_output(ctx, B.schema, P.schema, 0);
@@ -637,7 +653,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     {
         unsigned long long c[4] = {};
         PHJ_CUDA(cudaMemcpy(c, ctr, sizeof(c), cudaMemcpyDeviceToHost));
-        const float bs = event_ms(ev[0], ev[1]), bd = event_ms(ev[1], ev[2]), e2e = event_ms(ev[0], eb[0]);
+        const float bs = event_ms(ev[0], ev[1]), bd = event_ms(ev[1], ev[2]) + t_lazy, e2e = event_ms(ev[0], eb[0]);
         fill_phase(res->build_shuffle, bs, B.rows);
         fill_phase(res->build, bd, B.rows);
         fill_phase(res->probe_shuffle, t_shuffle, P.rows);
@@ -907,6 +923,7 @@ phj_status phj_ctx_create(int device, phj_ctx ** out)
         PHJ_CUDA(cudaMemset(ctx->d_err, 0, sizeof(int)));
         set_partition_smem_limits((int)ctx->smem_optin);
         set_build_smem_limits((int)ctx->smem_optin);
+        set_bep_smem_limits((int)ctx->smem_optin);
     });
     if (st != PHJ_OK)
     {
@@ -1232,6 +1249,11 @@ phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_tab
         check_sides(build, probe);
         if (bep_budget_mib == 0 || bep_budget_mib > (1ull << 30))
             throw Error(PHJ_ERR_INVALID_ARGUMENT, "bep_budget_mib must be in [1, 2^30]");
+        uint32_t total = 0;
+        for (uint32_t b : bits)
+            total += b;
+        if (total > 20)
+            throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) on the device takes at most 20 radix bits (2^20 leaves)");
         run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
     });
 }

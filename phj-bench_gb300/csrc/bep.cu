@@ -1,0 +1,213 @@
+// bep.cu -- lazy leaf tables of the PHJ (BEP) scheme: each leaf table is
+// built the first time a probe batch needs it.
+//
+// Per batch, before its lookups: k_bep_mark hashes the batch's probe keys
+// and flags the leaves they touch; k_bep_collect counts each touched leaf
+// as one eviction (its buffered rows are probed in this batch) and queues
+// the touched leaves that are not yet built.  k_bep_build is a persistent
+// grid whose CTAs take leaves from that queue: a CTA wins NOT_BUILT ->
+// BUILDING with a CAS, builds the table in shared memory with 128-bit CAS
+// inserts, threads the next-chain and publishes BUILT; a CTA that finds a
+// leaf BUILDING waits for it, bounded by a wall-clock limit, then gives up
+// with an error code.  The lookups that follow read only BUILT tables, from
+// a later kernel.
+#include "internal.h"
+
+namespace phjg
+{
+namespace
+{
+constexpr uint32_t kNotBuilt = 0, kBuilding = 1, kBuilt = 2, kBuiltDup = 3;
+constexpr int kBepNT = 256;
+constexpr uint32_t kBepSmemCellsMax = 8192; // 128 KiB of cells per CTA
+constexpr int kMarkNT = 512;
+constexpr size_t kBepMaxMarkLeaves = 1u << 20; // the CTA bitmap (128 KiB) bounds the leaf count
+
+__device__ __forceinline__ uint32_t load_acquire(const uint32_t * p)
+{
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ uint64_t global_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Marks the leaves a batch's probe keys touch in a bitmap.  Each CTA sets
+// bits of its own shared-memory copy (a bit is read before it is set, so
+// the hot leaves of a skewed probe side cost a shared-memory read) and ORs
+// the copy into the global bitmap at the end.
+__global__ void __launch_bounds__(kMarkNT) k_bep_mark(BepLeaves b, const uint64_t * __restrict__ keys, uint64_t n)
+{
+    extern __shared__ uint32_t bm[];
+    const uint32_t words = (b.n_leaves + 31) / 32;
+    for (uint32_t w = threadIdx.x; w < words; w += kMarkNT)
+        bm[w] = 0;
+    __syncthreads();
+    const uint32_t shift = 64u - b.leaf_bits;
+    const uint64_t stride = (uint64_t)gridDim.x * kMarkNT;
+    for (uint64_t i = (uint64_t)blockIdx.x * kMarkNT + threadIdx.x; i < n; i += 4 * stride)
+    {
+        uint32_t L[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint64_t r = i + u * stride;
+            L[u] = r < n ? (uint32_t)(int_hash64(__ldcs(keys + r)) >> shift) : 0xFFFFFFFFu;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            if (L[u] != 0xFFFFFFFFu && !(bm[L[u] >> 5] & (1u << (L[u] & 31))))
+                atomicOr(&bm[L[u] >> 5], 1u << (L[u] & 31));
+    }
+    __syncthreads();
+    for (uint32_t w = threadIdx.x; w < words; w += kMarkNT)
+        if (bm[w])
+            atomicOr(b.touched + w, bm[w]);
+}
+
+// One pass over the leaves, a warp per bitmap word: each touched leaf is one
+// eviction (its buffered rows are probed in this batch); touched leaves not
+// yet built are queued.  The word is cleared for the next batch.
+__global__ void k_bep_collect(BepLeaves b)
+{
+    const uint32_t L = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t word = 0;
+    if (lane == 0 && L < b.n_leaves)
+    {
+        word = b.touched[L >> 5];
+        b.touched[L >> 5] = 0;
+    }
+    word = __shfl_sync(0xffffffffu, word, 0);
+    const bool t = L < b.n_leaves && (word >> lane & 1u);
+    const bool q = t && b.state[L] < kBuilt;
+    const uint32_t tm = __ballot_sync(0xffffffffu, t), qm = __ballot_sync(0xffffffffu, q);
+    uint32_t base = 0;
+    if (lane == 0)
+    {
+        if (tm)
+            atomicAdd(b.ctr + 2, (unsigned long long)__popc(tm));
+        if (qm)
+            base = atomicAdd(b.queue_len, (uint32_t)__popc(qm));
+    }
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (q)
+        b.queue[base + __popc(qm & ((1u << lane) - 1u))] = L;
+}
+
+// A CTA per queued leaf: it wins NOT_BUILT -> BUILDING, builds the table in
+// shared memory (or in place when it is larger than `smem_cells`), copies it
+// out, threads the next-chain and publishes BUILT; or it finds the leaf
+// BUILDING and waits for it (bounded).
+__global__ void __launch_bounds__(kBepNT) k_bep_build(BepLeaves b, int * __restrict__ err)
+{
+    extern __shared__ __align__(16) Cell sh_cells[];
+    __shared__ uint32_t s_leaf, s_won, s_stop;
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+        {
+            const uint32_t idx = atomicAdd(b.queue_len + 1, 1u);
+            s_leaf = idx < *reinterpret_cast<volatile uint32_t *>(b.queue_len) ? b.queue[idx] : 0xFFFFFFFFu;
+            s_won = s_leaf != 0xFFFFFFFFu && atomicCAS(b.state + s_leaf, kNotBuilt, kBuilding) == kNotBuilt;
+            s_stop = 0;
+        }
+        __syncthreads();
+        const uint32_t L = s_leaf;
+        if (L == 0xFFFFFFFFu)
+            return;
+        if (s_won)
+        {
+            const LeafMeta m = b.meta[L];
+            bool dup = false;
+            if (m.has_table)
+            {
+                const uint64_t cap = 1ull << m.log2cap;
+                const bool in_smem = cap <= b.smem_cells;
+                Cell * tab = in_smem ? sh_cells : b.cells + m.table_off;
+                for (uint64_t i = threadIdx.x; i < cap; i += kBepNT)
+                    reinterpret_cast<ulonglong2 *>(tab)[i] = make_ulonglong2(0ull, INVALID_REF);
+                __syncthreads();
+                const uint32_t r0 = m.row_off, r1 = b.leaf_off[L + 1];
+                for (uint32_t r = r0 + threadIdx.x; r < r1; r += kBepNT)
+                {
+                    const uint64_t k = b.build_keys[r];
+                    const uint64_t h = int_hash64(k);
+                    const uint64_t prev = in_smem ? table_insert<true>(tab, cap, h, k, make_ref(0, r)) : table_insert<false>(tab, cap, h, k, make_ref(0, r));
+                    b.next[r] = prev;
+                    dup |= ref_valid(prev);
+                }
+                dup = __syncthreads_or(dup);
+                if (in_smem)
+                    for (uint64_t i = threadIdx.x; i < cap; i += kBepNT)
+                        reinterpret_cast<ulonglong2 *>(b.cells + m.table_off)[i] = reinterpret_cast<const ulonglong2 *>(sh_cells)[i];
+            }
+            __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0)
+            {
+                b.meta[L].dup = dup ? 1 : 0;
+                atomicExch(b.state + L, dup ? kBuiltDup : kBuilt);
+                atomicAdd(b.ctr + 0, 1ull);
+                if (dup)
+                    atomicExch(b.any_dup, 1);
+            }
+        }
+        else if (threadIdx.x == 0 && load_acquire(b.state + L) < kBuilt)
+        {
+            atomicAdd(b.ctr + 1, 1ull);
+            const uint64_t t0 = global_ns();
+            uint32_t spins = 0;
+            while (load_acquire(b.state + L) < kBuilt)
+                if (++spins >= kWaitLimit || global_ns() - t0 > b.wait_limit_ns)
+                {
+                    atomicExch(err, 4);
+                    s_stop = 1;
+                    break;
+                }
+        }
+        __syncthreads();
+        if (s_stop)
+            return;
+    }
+}
+} // namespace
+
+void set_bep_smem_limits(int smem_optin)
+{
+    PHJ_CUDA(cudaFuncSetAttribute(k_bep_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(kBepMaxMarkLeaves / 8, (size_t)smem_optin - 1024)));
+    PHJ_CUDA(cudaFuncSetAttribute(k_bep_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::min<size_t>((size_t)kBepSmemCellsMax * sizeof(Cell), (size_t)smem_optin - 1024)));
+}
+
+bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b, const uint64_t * probe_keys, uint64_t n)
+{
+    PHJ_CUDA(cudaMemsetAsync(b.queue_len, 0, 2 * sizeof(uint32_t), ctx->stream));
+    if (n)
+    {
+        KTimer kt(ctx, "bep_mark", n, n * 8);
+        const size_t bm_bytes = (size_t)((b.n_leaves + 31) / 32) * 4;
+        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(n, kMarkNT * 16), (uint64_t)ctx->num_sms * 2));
+        k_bep_mark<<<grid, kMarkNT, bm_bytes, ctx->stream>>>(b, probe_keys, n);
+        PHJ_LAUNCHED(ctx, "bep_mark");
+    }
+    k_bep_collect<<<(unsigned)ceil_div(b.n_leaves, kBepNT), kBepNT, 0, ctx->stream>>>(b);
+    PHJ_LAUNCHED(ctx, "bep_collect");
+    {
+        KTimer kt(ctx, "bep_build", 0, 0);
+        int per_sm = 0;
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bep_build, kBepNT, (size_t)b.smem_cells * sizeof(Cell)));
+        k_bep_build<<<(unsigned)(ctx->num_sms * std::max(per_sm, 1)), kBepNT, (size_t)b.smem_cells * sizeof(Cell), ctx->stream>>>(b, ctx->d_err);
+        PHJ_LAUNCHED(ctx, "bep_build");
+    }
+    int dup = 0;
+    PHJ_CUDA(cudaMemcpyAsync(&dup, b.any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    return dup != 0;
+}
+} // namespace phjg

@@ -237,19 +237,40 @@ struct ProbeArgs
     uint32_t uniform_block_rows;
     int any_dup;
     int uniform_log2cap;    // >= 0: PHJ leaf tables of uniform capacity (no directory lookup)
-    // Lazy leaf tables (PHJ/BEP): built by the first warp that needs one.
-    uint32_t * leaf_state;        // NOT_BUILT 0 -> BUILDING 1 -> BUILT 2 (3: BUILT, keys repeat)
-    const uint32_t * leaf_off;    // first build row of each leaf (n_leaves + 1)
-    const uint64_t * build_keys;  // leaf-partitioned build keys
-    uint32_t * leaf_epoch;        // last batch (1-based) that probed each leaf
-    uint32_t epoch;               // this batch
-    uint64_t wait_limit_ns;       // bound of a wait on a BUILDING leaf
-    unsigned long long * bep_ctr; // [0] tables built, [1] waits on BUILDING, [2] leaf evictions, [3] refinements
     // Grouped leaves (PHJ-PURE with repeated keys): a cell holds {count,
     // first row}; the lookup records each probe row's match count here.
     int grouped;
     uint32_t * row_cnt;
 };
+// PHJ/BEP lazy leaf tables.  Per probe batch: mark the leaves the batch
+// touches (one eviction per leaf and batch), queue the touched leaves still
+// NOT_BUILT, and let persistent warps take leaves from that queue and build
+// them (NOT_BUILT -> BUILDING -> BUILT; a leaf found BUILDING is waited for,
+// bounded by wait_limit_ns).  Counters: [0] tables built, [1] waits on a
+// BUILDING leaf, [2] evictions.
+struct BepLeaves
+{
+    uint32_t * state;             // per leaf: 0 NOT_BUILT, 1 BUILDING, 2 BUILT, 3 BUILT (keys repeat)
+    uint32_t * touched;           // bitmap over the leaves: touched by the current batch
+    const uint32_t * leaf_off;    // first build row of each leaf (n_leaves + 1)
+    const uint64_t * build_keys;  // leaf-partitioned build keys
+    LeafMeta * meta;
+    Cell * cells;
+    uint64_t * next;
+    uint32_t leaf_bits;
+    uint32_t n_leaves;
+    uint32_t smem_cells;          // tables up to this many cells are built in shared memory
+    uint64_t wait_limit_ns;
+    unsigned long long * ctr;
+    uint32_t * queue;             // n_leaves entries
+    uint32_t * queue_len;         // [0] queued leaves, [1] leaves taken
+    int * any_dup;                // set when a built leaf has a repeated key
+};
+// Builds the leaves the batch's probe keys touch.  Returns whether any leaf
+// built so far has a repeated key (the lookup then follows chains).
+bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b, const uint64_t * probe_keys, uint64_t n);
+void set_bep_smem_limits(int smem_optin);
+
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);
 // The two halves: lookups + chunk-offset scan (returns the output rows), and

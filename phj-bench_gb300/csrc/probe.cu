@@ -75,13 +75,13 @@ __device__ __forceinline__ uint32_t build_row_of(uint64_t ref, const ProbeArgs &
 }
 
 // Linear probing from cell `pos` on (the first cell collided).
-__device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t cap, uint64_t pos, uint64_t key, bool coherent = false)
+__device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t cap, uint64_t pos, uint64_t key)
 {
     const uint64_t mask = cap - 1;
     pos &= mask;
     for (uint64_t step = 1; step < cap; ++step)
     {
-        const ulonglong2 c = coherent ? __ldcg(reinterpret_cast<const ulonglong2 *>(cells + pos)) : __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
+        const ulonglong2 c = __ldg(reinterpret_cast<const ulonglong2 *>(cells + pos));
         if (!ref_valid(c.y))
             return INVALID_REF;
         if (c.x == key)
@@ -91,15 +91,15 @@ __device__ __noinline__ uint64_t table_find_from(const Cell * cells, uint64_t ca
     return INVALID_REF;
 }
 
-__device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj, bool coherent = false)
+__device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a, int chj)
 {
     uint32_t c = 1;
-    uint64_t r = coherent ? __ldcg(a.next + brow) : __ldg(a.next + brow);
+    uint64_t r = __ldg(a.next + brow);
     while (ref_valid(r))
     {
         ++c;
         const uint32_t b = chj ? build_row_of<kChj>(r, a) : build_row_of<kLeafMeta>(r, a);
-        r = coherent ? __ldcg(a.next + b) : __ldg(a.next + b);
+        r = __ldg(a.next + b);
     }
     return c;
 }
@@ -172,143 +172,11 @@ __device__ __forceinline__ void columns_pass(const Cols & src, void * const * ds
         }
 }
 
-// ---- lazy leaf tables (PHJ/BEP) --------------------------------------------
-// Leaf state: NOT_BUILT -> BUILDING -> BUILT (BUILT_DUP when a key repeats).
-constexpr uint32_t kNotBuilt = 0, kBuilding = 1, kBuilt = 2, kBuiltDup = 3;
-
-__device__ __forceinline__ uint32_t load_acquire(const uint32_t * p)
-{
-    uint32_t v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ uint64_t global_ns()
-{
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// The whole warp builds leaf L's table: clear the cells, insert the leaf's
-// build rows with 128-bit CAS, thread the next-chain.  Returns whether a
-// key repeats within the leaf.
-__device__ __noinline__ bool warp_build_leaf(const ProbeArgs & a, uint32_t L, uint32_t lane)
-{
-    const ulonglong2 mv = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + L));
-    if (!((mv.y >> 40) & 0xffu))
-        return false;
-    const uint64_t cap = 1ull << ((uint32_t)(mv.y >> 32) & 0xffu);
-    Cell * tab = const_cast<Cell *>(a.cells) + mv.x;
-    const uint32_t r0 = (uint32_t)mv.y;
-    const uint32_t r1 = __ldg(a.leaf_off + L + 1);
-    for (uint64_t i = lane; i < cap; i += 32)
-        reinterpret_cast<ulonglong2 *>(tab)[i] = make_ulonglong2(0ull, INVALID_REF);
-    __threadfence();
-    __syncwarp();
-    uint64_t * next = const_cast<uint64_t *>(a.next);
-    bool dup = false;
-    for (uint32_t r = r0 + lane; r < r1; r += 32)
-    {
-        const uint64_t k = __ldg(a.build_keys + r);
-        const uint64_t prev = table_insert<false>(tab, cap, int_hash64(k), k, make_ref(0, r));
-        next[r] = prev;
-        dup |= ref_valid(prev);
-    }
-    __threadfence();
-    return __any_sync(0xffffffffu, dup);
-}
-
-// Makes sure the leaves l[0..3] of a four-row group's live rows are built
-// and returns their states, two bits each.  The first warp to need a leaf
-// wins NOT_BUILT -> BUILDING, builds it and publishes BUILT; a warp that
-// finds it BUILDING waits, bounded by a wall-clock limit, and the wait is
-// counted.  Returns kStatesTimeout after a timeout (code 4 in *err).  Called
-// by the whole warp when some lane's leaf is not yet BUILT.
-constexpr uint32_t kStatesTimeout = 0xffffffffu;
-
-__device__ __noinline__ uint32_t ensure_built_slow(const ProbeArgs & a, uint32_t l0, uint32_t l1, uint32_t l2, uint32_t l3, uint32_t live4,
-                                                   uint32_t lane, int * err)
-{
-    const uint32_t leaf[4] = {l0, l1, l2, l3};
-    uint32_t st[4];
-    bool need[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u)
-    {
-        st[u] = (live4 >> u & 1u) ? load_acquire(a.leaf_state + leaf[u]) : kBuilt;
-        need[u] = st[u] < kBuilt;
-    }
-#pragma unroll 1
-    for (int u = 0; u < 4; ++u)
-    {
-        for (uint32_t m = __ballot_sync(0xffffffffu, need[u]); m; m = __ballot_sync(0xffffffffu, need[u]))
-        {
-            const int src = __ffs(m) - 1;
-            const uint32_t L = __shfl_sync(0xffffffffu, leaf[u], src);
-            uint32_t won = 0;
-            if ((int)lane == src)
-                won = atomicCAS(a.leaf_state + L, kNotBuilt, kBuilding) == kNotBuilt;
-            won = __shfl_sync(0xffffffffu, won, src);
-            uint32_t ok = 1;
-            if (won)
-            {
-                const bool dup = warp_build_leaf(a, L, lane);
-                if ((int)lane == src)
-                {
-                    atomicExch(a.leaf_state + L, dup ? kBuiltDup : kBuilt);
-                    atomicAdd(a.bep_ctr + 0, 1ull);
-                }
-            }
-            else if ((int)lane == src && load_acquire(a.leaf_state + L) < kBuilt)
-            {
-                const uint64_t t0 = global_ns();
-                uint32_t spins = 0;
-                while (load_acquire(a.leaf_state + L) < kBuilt)
-                    if (++spins >= kWaitLimit || global_ns() - t0 > a.wait_limit_ns)
-                    {
-                        atomicExch(err, 4);
-                        ok = 0;
-                        break;
-                    }
-                atomicAdd(a.bep_ctr + 1, 1ull);
-            }
-            ok = __shfl_sync(0xffffffffu, ok, src);
-            if (!ok)
-                return kStatesTimeout;
-#pragma unroll
-            for (int v = 0; v < 4; ++v)
-                if (need[v])
-                {
-                    st[v] = load_acquire(a.leaf_state + leaf[v]);
-                    need[v] = st[v] < kBuilt;
-                }
-        }
-    }
-    return st[0] | st[1] << 2 | st[2] << 4 | st[3] << 6;
-}
-
-// The batch a leaf was last probed in; the first row of a new batch to
-// reach a leaf counts one eviction (the leaf's buffered rows are probed).
-__device__ __forceinline__ void note_leaf_batch(const ProbeArgs & a, uint32_t L)
-{
-    if (*reinterpret_cast<const volatile uint32_t *>(a.leaf_epoch + L) != a.epoch && atomicExch(a.leaf_epoch + L, a.epoch) != a.epoch)
-        atomicAdd(a.bep_ctr + 2, 1ull);
-}
-// Cell / next-chain loads: through the non-coherent read-only path when the
-// tables were finished by an earlier kernel, through L2 when this kernel
-// may build them (lazy).
-template <bool kLazy>
-__device__ __forceinline__ ulonglong2 load_cell(const Cell * p)
-{
-    return kLazy ? __ldcg(reinterpret_cast<const ulonglong2 *>(p)) : __ldg(reinterpret_cast<const ulonglong2 *>(p));
-}
-
 // Lookups: per probe row its head build row (kNoMatch when the key is
 // absent), per warp chunk its number of output rows.
-template <int kMode, bool kDup, bool kLazy>
+template <int kMode, bool kDup>
 __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
-                                                       uint32_t * __restrict__ counts, int * __restrict__ err)
+                                                       uint32_t * __restrict__ counts)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -316,10 +184,10 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
     const uint32_t shift = 64u - a.leaf_bits;
     const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
     const uint64_t ucap = 1ull << ulog;
-    __shared__ uint64_t q_key[kLazy ? 1 : kPWarps * kWChunk];
-    __shared__ uint16_t q_row[kLazy ? 1 : kPWarps * kWChunk];
-    uint64_t * qkey = q_key + (kLazy ? 0 : (threadIdx.x >> 5) * kWChunk);
-    uint16_t * qrow = q_row + (kLazy ? 0 : (threadIdx.x >> 5) * kWChunk);
+    __shared__ uint64_t q_key[kPWarps * kWChunk];
+    __shared__ uint16_t q_row[kPWarps * kWChunk];
+    uint64_t * qkey = q_key + (threadIdx.x >> 5) * kWChunk;
+    uint16_t * qrow = q_row + (threadIdx.x >> 5) * kWChunk;
     for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
     {
         const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
@@ -351,32 +219,6 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                 if (kMode != kLeafUniform && (live >> (g + u) & 1u))
                     mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
             }
-            uint32_t st = 0xffu; // four states, two bits each (kBuiltDup: follow chains)
-            if (kLazy)
-            {
-                uint32_t leaf[4];
-                bool need = false;
-                st = 0;
-#pragma unroll
-                for (int u = 0; u < 4; ++u)
-                {
-                    leaf[u] = (uint32_t)(int_hash64(key[g + u]) >> shift);
-                    uint32_t v = kBuilt;
-                    if (live >> (g + u) & 1u)
-                    {
-                        note_leaf_batch(a, leaf[u]);
-                        v = load_acquire(a.leaf_state + leaf[u]);
-                    }
-                    need |= v < kBuilt;
-                    st |= v << (2 * u);
-                }
-                if (__any_sync(0xffffffffu, need))
-                {
-                    st = ensure_built_slow(a, leaf[0], leaf[1], leaf[2], leaf[3], (live >> g) & 0xfu, lane, err);
-                    if (st == kStatesTimeout)
-                        return;
-                }
-            }
             CellPair cell[4];
 #pragma unroll
             for (int u = 0; u < 4; ++u)
@@ -388,9 +230,9 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     continue;
                 const uint64_t h = int_hash64(key[k]);
                 if (kMode == kLeafUniform)
-                    cell[u] = load_pair<kLazy>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
+                    cell[u] = load_pair<false>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
                 else if ((mv[u].y >> 40) & 0xffu)
-                    cell[u] = load_pair<kLazy>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
+                    cell[u] = load_pair<false>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
             }
 #pragma unroll
             for (int u = 0; u < 4; ++u)
@@ -412,21 +254,6 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                             more = true;
                     }
                 }
-                if constexpr (kLazy)
-                {
-                    if (more)
-                    {
-                        const uint64_t h = int_hash64(key[k]);
-                        if (kMode == kLeafUniform)
-                            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, key[k], kLazy);
-                        else
-                        {
-                            const uint64_t c = 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu);
-                            head = table_find_from(a.cells + mv[u].x, c, probe_start(h, c) + 2, key[k], kLazy);
-                        }
-                    }
-                }
-                else
                 {
                     // rows whose key lies past the cell pair wait in the
                     // warp's queue and are probed together after the chunk
@@ -439,28 +266,27 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     }
                     qn += __popc(m);
                 }
-                if (!more || kLazy)
+                if (!more)
                 {
                     if (ref_valid(head))
                     {
                         brow = build_row_of<kMode>(head, a);
-                        const bool leaf_dup = kLazy ? ((st >> (2 * u)) & 3u) == kBuiltDup : kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
-                        if (kDup && kMode != kChj && !kLazy && a.grouped)
+                        const bool leaf_dup = kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
+                        if (kDup && kMode != kChj && a.grouped)
                             mcnt = ref_block(head) ? ref_block(head) : 1u; // grouped: {count, first row}
                         else
-                            mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj, kLazy) : 1u;
+                            mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
                         total += mcnt;
                     }
                 }
-                if ((live >> k & 1u) && (!more || kLazy))
+                if ((live >> k & 1u) && !more)
                 {
                     heads[row0 + (uint64_t)k * 32] = brow;
-                    if (kDup && kMode != kChj && !kLazy && a.grouped)
+                    if (kDup && kMode != kChj && a.grouped)
                         a.row_cnt[row0 + (uint64_t)k * 32] = mcnt;
                 }
             }
         }
-        if constexpr (!kLazy)
         {
             __syncwarp();
             for (uint32_t j = lane; j < qn; j += 32)
@@ -737,8 +563,7 @@ template <int kMode, bool kDup>
 static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, uint32_t * heads, uint32_t * counts, uint64_t cap, bool lookup,
                          const char * name, uint64_t bytes)
 {
-    const bool lazy = a.leaf_state != nullptr;
-    auto lk = lazy ? k_probe_lookup<kMode, kDup, true> : k_probe_lookup<kMode, kDup, false>;
+    auto lk = k_probe_lookup<kMode, kDup>;
     bool grouped = false;
     if constexpr (kDup && kMode != kChj)
         grouped = a.grouped != 0;
@@ -760,7 +585,7 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
         throw Error(PHJ_ERR_CUDA, "internal: leaf tables need aligned pairs of cells");
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
-        lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts, ctx->d_err);
+        lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
     else
     {
         if (!grouped)

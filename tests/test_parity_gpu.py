@@ -219,11 +219,14 @@ def test_bep_stuck_leaf_times_out_and_context_recovers(ctx):
     check(b, p, jo, fp)
 
 
-def test_bep_invalid_budget(ctx):
+def test_bep_invalid_budget_and_too_many_leaves(ctx):
     b, p = cases.make("c2_mini")
     tb, tp = ctx.upload(b), ctx.upload(p)
     with pytest.raises(P.PhjError):
         ctx.run_phj_bep(tb, tp, [4], 0)
+    with pytest.raises(P.PhjError) as e:
+        ctx.run_phj_bep(tb, tp, [11, 10], 1)
+    assert e.value.status == 4  # PHJ_ERR_UNSUPPORTED
     tb.free(), tp.free()
 
 
