@@ -258,23 +258,23 @@ def run_scheme(ctx, scheme, b, p, bits, budget_mib=0):
     return ctx.run_phj_pure(b, p, bits)
 
 
-def cpu_scheme(scheme):
-    """The CPU port covers CHJ and PHJ-PURE; PHJ (BEP) is timed as PHJ-PURE,
-    the same partitioned join without the probe budget."""
-    return "phj-pure" if scheme == "phj" else scheme
+def cpu_budget_mib(workload, threads):
+    """PHJ (BEP) budget of the CPU run: the per-worker budget times the
+    worker threads (the GPU run gives each CTA group the same share)."""
+    return BEP_BUDGET_PER_GROUP.get(workload, 32) * threads
 
 
-def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3):
+def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3, budget_mib=512):
     import oracle
     n_p = max(1, int(len(phost.keys) * frac))
     probe = type(phost)(phost.types, phost.keys[:n_p], [c[:n_p] for c in phost.payloads])
     times = []
     for _ in range(reps):
-        _, ms = oracle.port_run(cpu_scheme(scheme), bhost, probe, bits, threads)
+        _, ms = oracle.port_run(scheme, bhost, probe, bits, threads, budget_mib)
         times.append(ms["e2e"])
     t = statistics.median(times) / 1e3
     return {"value": (len(bhost.keys) + n_p) / t, "unit": "tuples/s", "cores": threads, "kind": "port",
-            "sample": f"{cpu_scheme(scheme)} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
+            "sample": f"{scheme} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
                       f"({frac:.4g} of the probe side); median of {reps} runs, {threads} host threads; "
                       f"C++ port of the reference's scheme (oracle/cpu_port.cpp)",
             "ms_per_run": statistics.median(times)}
@@ -308,12 +308,13 @@ def reference_arm(args, rank, world, dist):
     else:
         pk = G.gen_keys(pspec["kind"], n_p, pspec["seed"], pspec["key_seed"], domain=dom)
     p = P.BlockStream(pspec["types"], pk, G.payload_columns(pspec["seed"], pspec["types"], n_p))
-    cs = cpu_scheme(scheme)
+    cs = scheme
+    budget = cpu_budget_mib(args.workload, threads)
     for _ in range(args.warmup):
-        oracle.port_run(cs, b, p, bits, threads)
+        oracle.port_run(cs, b, p, bits, threads, budget)
     times = []
     for _ in range(args.steps):
-        _, ms = oracle.port_run(cs, b, p, bits, threads)
+        _, ms = oracle.port_run(cs, b, p, bits, threads, budget)
         times.append(ms["e2e"])
     t = statistics.mean(times)
     value = (len(b.keys) + n_p) / (t / 1e3)
@@ -511,7 +512,9 @@ def main():
     # -------- CPU baseline (rank 0, N = 1 only) --------
     if rank == 0 and world == 1 and not args.no_cpu:
         try:
-            line["cpu_baseline"] = cpu_baseline(hb, hp, bits, args.cpu_probe_frac, os.cpu_count() or 1, scheme)
+            ncpu = os.cpu_count() or 1
+            line["cpu_baseline"] = cpu_baseline(hb, hp, bits, args.cpu_probe_frac, ncpu, scheme,
+                                                budget_mib=cpu_budget_mib(args.workload, ncpu))
         except Exception as e:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"value": None, "error": str(e)}
     b.free(), p.free()

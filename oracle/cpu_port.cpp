@@ -643,3 +643,306 @@ extern "C" int64_t port_run_chj(const port_stream * build, const port_stream * p
     }
     return total;
 }
+
+// ---------------------------------------------------------------------------
+// runPhjBep, src/PHJBep.cpp:113-790: full-depth build shuffle, eager leaf
+// tables; per worker, its slice of probe blocks is scattered by pass 1 into
+// private chains; a chain is refined to leaf depth (passes 2..N) into shared
+// per-leaf chains when the worker's private bytes pass half its share of the
+// budget (down to a quarter); shared leaves are evicted (probed and dropped)
+// round-robin with try-lock once they hold 5/8 of the budget (down to 5/8 of
+// that); finished workers help evict while others still scatter; residual
+// private chains are refined and every leaf is drained at the end.
+// ---------------------------------------------------------------------------
+namespace
+{
+struct BepLeaf
+{
+    std::mutex mu;
+    std::vector<OutBlk> blocks;
+    std::atomic<size_t> rows{0};
+};
+
+// refineToLeaves: passes 2..N of one pass-1 chain (src/RadixPartition.cpp:417-539)
+void refine_chain(std::vector<OutBlk> && in, const Schema & s, const std::vector<uint32_t> & bits, std::vector<Chain> & out_leaves, Scratch & sc)
+{
+    std::vector<std::vector<OutBlk>> cur(1);
+    cur[0] = std::move(in);
+    uint32_t consumed = bits[0];
+    size_t parts = 1;
+    for (size_t pass = 1; pass < bits.size(); ++pass)
+    {
+        const size_t sub = size_t{1} << bits[pass];
+        const uint32_t shift = 64u - consumed - bits[pass];
+        std::vector<Chain> next(parts * sub);
+        for (auto & c : next)
+            c.next_cap = s.initial_rows();
+        for (size_t ip = 0; ip < parts; ++ip)
+            for (const OutBlk & ob : cur[ip])
+                scatter_batch(ob.view(), s, shift, sub, next.data() + ip * sub, sc);
+        cur.assign(parts * sub, {});
+        for (size_t p = 0; p < parts * sub; ++p)
+            for (auto & b : next[p].blocks)
+                if (b.rows)
+                    cur[p].push_back(std::move(b));
+        parts *= sub;
+        consumed += bits[pass];
+    }
+    out_leaves.assign(parts, Chain{});
+    for (size_t p = 0; p < parts; ++p)
+        out_leaves[p].blocks = std::move(cur[p]);
+}
+} // namespace
+
+extern "C" int64_t port_run_phj_bep(const port_stream * build, const port_stream * probe, const uint8_t * pass_bits, uint32_t n_passes,
+                                    uint32_t threads, uint64_t budget_mib, double * phase_ms, uint64_t * counters)
+{
+    if (!build || !probe || !pass_bits || n_passes == 0 || budget_mib == 0)
+        return -1;
+    threads = std::max(1u, threads);
+    const std::vector<uint32_t> bits(pass_bits, pass_bits + n_passes);
+    const Schema bs = schema_of(*build), ps = schema_of(*probe);
+    const auto t0 = Clock::now();
+    Partitions bpart = radix_shuffle(*build, bs, bits, threads);
+    const double t_bs = ms_since(t0);
+    const size_t total_leaves = bpart.size();
+    const size_t P = size_t{1} << bits[0];
+    const size_t leaves_per_p1 = total_leaves / P;
+    size_t bpr = 8;
+    for (uint32_t w : ps.w)
+        bpr += w;
+    const size_t budget = (size_t)budget_mib << 20;
+    const size_t per_worker = budget / threads;
+    const size_t unref_high = per_worker / 2, unref_low = unref_high / 2;
+    const size_t leaf_high = budget * 5 / 8, leaf_low = leaf_high * 5 / 8;
+
+    // eager leaf tables, work-stealing over leaves
+    const auto tb0 = Clock::now();
+    std::vector<Store> stores(total_leaves);
+    std::vector<Table> tables(total_leaves);
+    {
+        std::atomic<size_t> next{0};
+        run_threads(threads, [&](uint32_t) {
+            std::vector<uint64_t> hashes;
+            for (;;)
+            {
+                const size_t L = next.fetch_add(1, std::memory_order_relaxed);
+                if (L >= total_leaves)
+                    break;
+                size_t rows = 0;
+                for (const auto & b : bpart[L])
+                    rows += b.rows;
+                if (!rows)
+                    continue;
+                tables[L].reserve(rows);
+                for (const auto & b : bpart[L])
+                    build_block(b.view(), stores[L], tables[L], hashes);
+            }
+        });
+    }
+    const double t_build = ms_since(tb0);
+
+    std::vector<BepLeaf> leaves(total_leaves);
+    std::atomic<size_t> global_rows{0}, cursor{0}, peak{0}, active{threads};
+    std::atomic<uint64_t> evictions{0}, refinements{0}, skips{0};
+    std::vector<Materialiser> mats(threads);
+    std::vector<double> shuffle_ms(threads, 0), probe_ms(threads, 0), evict_ms(threads, 0);
+    const size_t block_rows = probe->block_rows ? probe->block_rows : 10000;
+    const size_t n_blocks = (probe->rows + block_rows - 1) / block_rows;
+    auto probe_leaf = [&](std::vector<OutBlk> & blocks, size_t L, Materialiser & mat, ProbeScratch & scr) {
+        if (!stores[L].blocks.empty())
+            for (const auto & b : blocks)
+                probe_block(b.view(), stores[L], tables[L], mat, scr);
+        blocks.clear();
+    };
+    // one round-robin eviction attempt; returns the rows evicted
+    auto try_evict = [&](uint32_t tid, Materialiser & mat, ProbeScratch & scr) -> size_t {
+        const auto te = Clock::now();
+        const size_t L = cursor.fetch_add(1, std::memory_order_relaxed) % total_leaves;
+        BepLeaf & lf = leaves[L];
+        if (lf.rows.load(std::memory_order_relaxed) == 0)
+        {
+            evict_ms[tid] += ms_since(te);
+            return 0;
+        }
+        std::unique_lock<std::mutex> lock(lf.mu, std::try_to_lock);
+        if (!lock.owns_lock())
+        {
+            skips.fetch_add(1, std::memory_order_relaxed);
+            evict_ms[tid] += ms_since(te);
+            return 0;
+        }
+        const size_t rows = lf.rows.load(std::memory_order_relaxed);
+        if (!rows)
+            return 0;
+        std::vector<OutBlk> stolen = std::move(lf.blocks);
+        lf.blocks.clear();
+        lf.rows.store(0, std::memory_order_relaxed);
+        lock.unlock();
+        global_rows.fetch_sub(rows, std::memory_order_relaxed);
+        evict_ms[tid] += ms_since(te);
+        const auto tp = Clock::now();
+        probe_leaf(stolen, L, mat, scr);
+        probe_ms[tid] += ms_since(tp);
+        evictions.fetch_add(1, std::memory_order_relaxed);
+        return rows;
+    };
+
+    run_threads(threads, [&](uint32_t tid) {
+        Materialiser & mat = mats[tid];
+        mat.ls = &bs;
+        mat.rs = &ps;
+        ProbeScratch scr;
+        Scratch sc, rsc;
+        std::vector<Chain> unref(P);
+        for (auto & c : unref)
+            c.next_cap = ps.initial_rows();
+        std::vector<size_t> unref_rows(P, 0);
+        size_t unref_bytes = 0;
+        std::vector<Chain> inter;
+        auto refine = [&](size_t p1) {
+            std::vector<OutBlk> blocks;
+            for (auto & b : unref[p1].blocks)
+                if (b.rows)
+                    blocks.push_back(std::move(b));
+            unref[p1] = Chain{};
+            unref[p1].next_cap = ps.initial_rows();
+            unref_bytes -= unref_rows[p1] * bpr;
+            unref_rows[p1] = 0;
+            refine_chain(std::move(blocks), ps, bits, inter, rsc);
+            size_t added_total = 0;
+            for (size_t i = 0; i < inter.size(); ++i)
+            {
+                size_t added = 0;
+                for (const auto & b : inter[i].blocks)
+                    added += b.rows;
+                if (!added)
+                    continue;
+                BepLeaf & lf = leaves[p1 * leaves_per_p1 + i];
+                std::lock_guard<std::mutex> lock(lf.mu);
+                for (auto & b : inter[i].blocks)
+                    if (b.rows)
+                        lf.blocks.push_back(std::move(b));
+                lf.rows.fetch_add(added, std::memory_order_relaxed);
+                added_total += added;
+            }
+            global_rows.fetch_add(added_total, std::memory_order_relaxed);
+            refinements.fetch_add(1, std::memory_order_relaxed);
+        };
+        const size_t b0 = n_blocks * tid / threads, b1 = n_blocks * (tid + 1) / threads;
+        for (size_t blk = b0; blk < b1; ++blk)
+        {
+            const auto ts = Clock::now();
+            View v;
+            const size_t r0 = blk * block_rows;
+            v.rows = std::min(block_rows, probe->rows - r0);
+            v.keys = probe->keys + r0;
+            for (size_t c = 0; c < ps.w.size(); ++c)
+                v.cols[c] = static_cast<const uint8_t *>(probe->cols[c]) + r0 * ps.w[c];
+            scatter_batch(v, ps, 64u - bits[0], P, unref.data(), sc);
+            for (size_t p = 0; p < P; ++p)
+                unref_rows[p] += sc.hist[p];
+            unref_bytes += v.rows * bpr;
+            const size_t cur = global_rows.load(std::memory_order_relaxed) * bpr;
+            size_t old = peak.load(std::memory_order_relaxed);
+            while (cur > old && !peak.compare_exchange_weak(old, cur, std::memory_order_relaxed))
+            {
+            }
+            // private chains above the high-water mark: refine the largest
+            if (unref_bytes >= unref_high)
+                while (unref_bytes >= unref_low)
+                {
+                    size_t best = SIZE_MAX, best_rows = 0;
+                    for (size_t p = 0; p < P; ++p)
+                        if (unref_rows[p] > best_rows)
+                            best_rows = unref_rows[p], best = p;
+                    if (best == SIZE_MAX)
+                        break;
+                    refine(best);
+                }
+            shuffle_ms[tid] += ms_since(ts);
+            // shared leaves above the high-water mark: evict
+            size_t cached = global_rows.load(std::memory_order_relaxed) * bpr;
+            if (cached >= leaf_high)
+            {
+                size_t misses = 0, since = 0;
+                while (cached >= leaf_low)
+                {
+                    const size_t rows = try_evict(tid, mat, scr);
+                    if (!rows)
+                    {
+                        if (++misses >= 64)
+                        {
+                            cached = global_rows.load(std::memory_order_relaxed) * bpr;
+                            misses = 0;
+                        }
+                        continue;
+                    }
+                    misses = 0;
+                    cached = cached > rows * bpr ? cached - rows * bpr : 0;
+                    if (++since >= 4)
+                    {
+                        cached = global_rows.load(std::memory_order_relaxed) * bpr;
+                        since = 0;
+                    }
+                }
+            }
+        }
+        // help evict while other workers still scatter
+        active.fetch_sub(1, std::memory_order_acq_rel);
+        while (active.load(std::memory_order_acquire) > 0)
+        {
+            if (global_rows.load(std::memory_order_relaxed) * bpr >= leaf_low && try_evict(tid, mat, scr))
+                continue;
+            std::this_thread::yield();
+        }
+        const auto tf = Clock::now();
+        for (size_t p = 0; p < P; ++p)
+            if (unref_rows[p])
+                refine(p);
+        shuffle_ms[tid] += ms_since(tf);
+    });
+    // drain every leaf, work-stealing
+    {
+        std::atomic<size_t> next{0};
+        run_threads(threads, [&](uint32_t tid) {
+            Materialiser & mat = mats[tid];
+            ProbeScratch scr;
+            for (;;)
+            {
+                const size_t L = next.fetch_add(1, std::memory_order_relaxed);
+                if (L >= total_leaves)
+                    break;
+                if (leaves[L].rows.load(std::memory_order_relaxed) == 0)
+                    continue;
+                const auto tp = Clock::now();
+                probe_leaf(leaves[L].blocks, L, mat, scr);
+                leaves[L].rows.store(0, std::memory_order_relaxed);
+                probe_ms[tid] += ms_since(tp);
+                evictions.fetch_add(1, std::memory_order_relaxed);
+            }
+            mat.finish();
+        });
+    }
+    const double e2e = ms_since(t0);
+    int64_t total = 0;
+    for (auto & m : mats)
+        total += (int64_t)m.total;
+    if (phase_ms)
+    {
+        phase_ms[0] = t_bs;
+        phase_ms[1] = t_build;
+        phase_ms[2] = *std::max_element(shuffle_ms.begin(), shuffle_ms.end());
+        phase_ms[3] = *std::max_element(probe_ms.begin(), probe_ms.end());
+        phase_ms[4] = *std::max_element(evict_ms.begin(), evict_ms.end());
+        phase_ms[5] = e2e;
+    }
+    if (counters)
+    {
+        counters[0] = evictions.load();
+        counters[1] = refinements.load();
+        counters[2] = peak.load();
+        counters[3] = skips.load();
+    }
+    return total;
+}

@@ -11,6 +11,7 @@
  *   buildOneBlock / probeOneBlock / materialiser   src/JoinOps.h:52-272
  *   runPHJ work-stealing over partitions           src/PHJ.cpp:19-150
  *   runCHJ slotted table, try-lock build           src/CHJ.cpp:16-119, src/JoinOps.h:290-429
+ *   runPhjBep budgeted probe buffering, eviction   src/PHJBep.cpp:113-790
  */
 #ifndef PHJ_CPU_PORT_H
 #define PHJ_CPU_PORT_H
@@ -34,6 +35,12 @@ typedef struct port_stream {
  * Returns output rows (materialised, then dropped), or -1 on bad arguments. */
 int64_t port_run_phj_pure(const port_stream *build, const port_stream *probe, const uint8_t *pass_bits, uint32_t n_passes,
                           uint32_t threads, double *phase_ms);
+
+/* phase_ms: [0] build_shuffle, [1] build, [2] probe_shuffle, [3] probe,
+ * [4] eviction_overhead, [5] e2e; counters: [0] evictions, [1] refinements,
+ * [2] peak buffered leaf bytes, [3] skipped try-locks. */
+int64_t port_run_phj_bep(const port_stream *build, const port_stream *probe, const uint8_t *pass_bits, uint32_t n_passes,
+                         uint32_t threads, uint64_t budget_mib, double *phase_ms, uint64_t *counters);
 
 /* phase_ms: [0] build, [1] probe, [2] e2e. */
 int64_t port_run_chj(const port_stream *build, const port_stream *probe, uint32_t threads, double *phase_ms);
