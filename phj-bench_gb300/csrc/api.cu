@@ -369,6 +369,15 @@ bool materialize_probe(phj_ctx * ctx, const LeafTables & lt, const phj_table & b
     return table_bytes + build_bytes > ctx->l2_bytes / 2;
 }
 
+// The same decision before the build: cells at load 1/2 (32 B per build
+// row) plus the build rows against half of L2.
+bool materialize_probe_estimate(phj_ctx * ctx, const phj_table & build)
+{
+    if (ctx->probe_materialize >= 0)
+        return ctx->probe_materialize != 0;
+    return build.rows * (32 + 8 + schema_bytes(build.schema)) > ctx->l2_bytes / 2;
+}
+
 Cols payload_cols(const Cols & c)
 {
     Cols p = c;
@@ -447,40 +456,71 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     for (uint32_t b : bits)
         total_bits += b;
     const uint32_t n_leaves = 1u << total_bits;
-    cudaEvent_t ev[5];
+    cudaEvent_t ev[7];
     for (auto & e : ev)
         e = take_event(ctx);
     PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+
+    // -------- PROBE SHUFFLE (src/PHJ.cpp:225-228): first pass only, on the
+    // side stream, beside the build side's work --------
+    ProbeArgs a{};
+    a.probe = cols_of(P);
+    const bool mat = materialize_probe_estimate(ctx, B) && P.rows > 0;
+    cudaStream_t main_stream = ctx->stream;
+    if (mat)
+    {
+        if (!ctx->side)
+            PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        PHJ_CUDA(cudaStreamWaitEvent(ctx->side, ev[0], 0));
+        ctx->stream = ctx->side;
+        try
+        {
+            PHJ_CUDA(cudaEventRecord(ev[5], ctx->stream));
+            const Cols ppart = alloc_cols_like(s, P.schema, P.rows);
+            const bool split = bits[0] > 11;
+            const Cols ptmp = split ? alloc_cols_like(s, P.schema, P.rows) : ppart;
+            uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
+            radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            a.probe = ppart;
+            PHJ_CUDA(cudaEventRecord(ev[6], ctx->stream));
+        }
+        catch (...)
+        {
+            ctx->stream = main_stream;
+            cudaStreamSynchronize(ctx->side);
+            throw;
+        }
+        ctx->stream = main_stream;
+    }
 
     // -------- BUILD SHUFFLE (src/PHJ.cpp:220-223) --------
     const Cols bin = cols_of(B);
     const Cols bpart = alloc_cols_like(s, B.schema, B.rows);
     const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
     uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
-    radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
-    PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
-
-    // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
     LeafTables lt;
-    lt.next = s.get<uint64_t>(B.rows);
-    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
-    // repeated keys: each key's rows made contiguous, so the probe expands a
-    // match as a row range
-    const bool grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
-    PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
-
-    // -------- PROBE SHUFFLE (src/PHJ.cpp:225-228): first pass only --------
-    ProbeArgs a{};
-    a.probe = cols_of(P);
-    if (materialize_probe(ctx, lt, B, n_leaves) && P.rows > 0)
+    bool grouped = false;
+    try
     {
-        const Cols ppart = alloc_cols_like(s, P.schema, P.rows);
-        const bool split = bits[0] > 11;
-        const Cols ptmp = split ? alloc_cols_like(s, P.schema, P.rows) : ppart;
-        uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
-        radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
-        a.probe = ppart;
+        radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+        PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+
+        // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
+        lt.next = s.get<uint64_t>(B.rows);
+        build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
+        // repeated keys: each key's rows made contiguous, so the probe
+        // expands a match as a row range
+        grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
+        PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
     }
+    catch (...)
+    {
+        if (mat)
+            cudaStreamSynchronize(ctx->side); // its buffers are freed with the scratch
+        throw;
+    }
+    if (mat)
+        PHJ_CUDA(cudaStreamWaitEvent(ctx->stream, ev[6], 0));
     PHJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
 
     // -------- PROBE with projection (src/PHJ.cpp:284-299) --------
@@ -502,7 +542,8 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     {
         fill_phase(res->build_shuffle, event_ms(ev[0], ev[1]), B.rows);
         fill_phase(res->build, event_ms(ev[1], ev[2]), B.rows);
-        fill_phase(res->probe_shuffle, event_ms(ev[2], ev[3]), P.rows);
+        // the probe side's first pass runs beside the build: its own span
+        fill_phase(res->probe_shuffle, mat ? event_ms(ev[5], ev[6]) : 0.f, P.rows);
         fill_phase(res->probe, event_ms(ev[3], ev[4]), P.rows);
         res->e2e_wall_ms = event_ms(ev[0], ev[4]);
         res->peak_mem_bytes = ctx->peak_bytes;
@@ -960,6 +1001,8 @@ void phj_ctx_destroy(phj_ctx * ctx)
         cudaStreamDestroy(ctx->h2d);
     if (ctx->d2h)
         cudaStreamDestroy(ctx->d2h);
+    if (ctx->side)
+        cudaStreamDestroy(ctx->side);
     delete ctx;
 }
 
