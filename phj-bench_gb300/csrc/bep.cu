@@ -147,7 +147,8 @@ __global__ void __launch_bounds__(kBepNT) k_bep_build(BepLeaves b, int * __restr
                     for (uint64_t i = threadIdx.x; i < cap; i += kBepNT)
                         reinterpret_cast<ulonglong2 *>(b.cells + m.table_off)[i] = reinterpret_cast<const ulonglong2 *>(sh_cells)[i];
             }
-            __threadfence();
+            // the tables are read by the lookups of a later kernel, so
+            // BUILT needs no fence for them; it only releases waiters
             __syncthreads();
             if (threadIdx.x == 0)
             {

@@ -332,6 +332,10 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
 // The projection walks a warp chunk in halves of kPH rounds (to bound
 // registers); the output offset carries over from one half to the next.
 constexpr int kPH = 4;
+// grouped projection: four CTAs of 256 threads per SM (at most 64
+// registers a thread) keep more gathers in flight than three CTAs with more
+// registers each (measured; the plain projection is faster at three)
+constexpr int kProjMinBlocks = 4;
 
 // One column over a lane's single-match rows of a half: four loads, then
 // four stores.  Output row of round k is base + rel[k].
@@ -468,7 +472,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
 // every output row costs the same whatever the match counts, and the
 // stores of a step are consecutive.
 template <int kMode>
-__global__ void __launch_bounds__(kPNT) k_probe_project_grouped(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+__global__ void __launch_bounds__(kPNT, kProjMinBlocks) k_probe_project_grouped(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
                                                                 const uint32_t * __restrict__ heads, const uint32_t * __restrict__ offs,
                                                                 uint64_t out_cap)
 {
