@@ -638,6 +638,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
     uint32_t * heads = s.get<uint32_t>(batch_rows);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(batch_rows) + 1);
+    a.row_cnt = s.get<uint32_t>(batch_rows); // match counts when keys repeat
     phj_output * o = nullptr;
     uint64_t total = 0, peak_rows = 0;
     float t_shuffle = 0.f, t_probe = 0.f, t_lazy = 0.f;
@@ -809,7 +810,7 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
     uint32_t * heads = s.get<uint32_t>(C);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(C) + 1);
-    if (grouped)
+    if (grouped || lt.any_dup)
         a.row_cnt = s.get<uint32_t>(C);
 
     // -------- PROBE, chunk by chunk --------

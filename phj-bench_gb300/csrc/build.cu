@@ -255,10 +255,14 @@ __global__ void k_chj_insert(const uint64_t * __restrict__ keys, uint64_t n, uin
         const LeafMeta m = meta[s];
         const uint64_t prev = table_insert<false>(cells + m.table_off, 1ull << m.log2cap, h, k, make_ref(b, row));
         next[g] = prev;
+        // flags read before they are written: a repeated key must not make
+        // every thread store to the same two addresses
         if (ref_valid(prev))
         {
-            meta[s].dup = 1; // idempotent byte store
-            *any_dup = 1;
+            if (!*reinterpret_cast<volatile uint8_t *>(&meta[s].dup))
+                meta[s].dup = 1;
+            if (!*reinterpret_cast<volatile int *>(any_dup))
+                *any_dup = 1;
         }
     }
 }

@@ -241,7 +241,8 @@ struct ProbeArgs
     // Grouped leaves (PHJ-PURE with repeated keys): a cell holds {count,
     // first row}; the lookup records each probe row's match count here.
     int grouped;
-    uint32_t * row_cnt;
+    uint32_t * row_cnt;  // per probe row: its match count (when keys repeat)
+    uint32_t * flat;     // chained duplicates: build row of every output row
 };
 // PHJ/BEP lazy leaf tables.  Per probe batch: mark the leaves the batch
 // touches (one eviction per leaf and batch), queue the touched leaves still

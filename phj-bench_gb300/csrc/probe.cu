@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                 if ((live >> k & 1u) && !more)
                 {
                     heads[row0 + (uint64_t)k * 32] = brow;
-                    if (kDup && kMode != kChj && a.grouped)
+                    if (kDup && a.row_cnt)
                         a.row_cnt[row0 + (uint64_t)k * 32] = mcnt;
                 }
             }
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
                     total += mcnt;
                 }
                 heads[row] = brow;
-                if (kDup && kMode != kChj && a.grouped)
+                if (kDup && a.row_cnt)
                     a.row_cnt[row] = mcnt;
             }
             __syncwarp();
@@ -465,13 +465,58 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
         }
     }
 }
+// Chained duplicates (CHJ, leaves too large to group, lazily built BEP
+// tables): each probe row's chain is walked once and its build rows are
+// written to a flat array at the row's output offsets, which the range
+// projection then reads in output order.
+template <int kMode>
+__global__ void __launch_bounds__(kPNT) k_probe_expand(const __grid_constant__ ProbeArgs a, const uint32_t * __restrict__ heads,
+                                                       const uint32_t * __restrict__ offs, uint64_t out_cap)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
+    for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
+    {
+        uint64_t base = offs[chunk];
+#pragma unroll 1
+        for (int k = 0; k < kPRPT; ++k)
+        {
+            const uint64_t row = chunk * kWChunk + (uint64_t)k * 32 + lane;
+            uint32_t b = kNoMatch, cnt = 0;
+            if (row < a.probe_rows)
+            {
+                b = __ldcs(heads + row);
+                if (b != kNoMatch)
+                    cnt = __ldcs(a.row_cnt + row);
+            }
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= (uint32_t)d)
+                    incl += y;
+            }
+            uint64_t o = base + incl - cnt;
+            for (uint32_t i = 0; i < cnt && o < out_cap; ++i, ++o)
+            {
+                a.flat[o] = b;
+                if (i + 1 < cnt)
+                    b = build_row_of<kMode>(__ldg(a.next + b), a);
+            }
+            base += __shfl_sync(0xffffffffu, incl, 31);
+        }
+    }
+}
+
 // Projection over grouped leaves: a probe row's matches are the build rows
 // [first, first + count).  Each round of 32 probe rows expands into its
 // output rows four per lane per step; a lane finds the probe row that owns
 // output j by a binary search over the warp's inclusive count prefix, so
 // every output row costs the same whatever the match counts, and the
 // stores of a step are consecutive.
-template <int kMode>
+template <int kMode, bool kFlat>
 __global__ void __launch_bounds__(kPNT, kProjMinBlocks) k_probe_project_grouped(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
                                                                 const uint32_t * __restrict__ heads, const uint32_t * __restrict__ offs,
                                                                 uint64_t out_cap)
@@ -522,7 +567,10 @@ __global__ void __launch_bounds__(kPNT, kProjMinBlocks) k_probe_project_grouped(
                     L = L > 31 ? 31 : L;
                     const uint32_t f = __shfl_sync(0xffffffffu, first, L);
                     const uint32_t e = __shfl_sync(0xffffffffu, excl, L);
-                    brow[u] = f + (j - e);
+                    if (kFlat)
+                        brow[u] = j < T ? __ldcs(a.flat + base + j) : 0u; // expanded chain
+                    else
+                        brow[u] = f + (j - e);
                     prow[u] = (uint32_t)(chunk * kWChunk + (uint64_t)k * 32 + L);
                     rel[u] = j;
                     if (j < T && base + j < out_cap)
@@ -568,35 +616,40 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
                          const char * name, uint64_t bytes)
 {
     auto lk = k_probe_lookup<kMode, kDup>;
-    bool grouped = false;
-    if constexpr (kDup && kMode != kChj)
-        grouped = a.grouped != 0;
+    // projection: plain (no repeated keys), range (grouped leaves) or flat
+    // (chains expanded first)
+    const int proj = !kDup ? 0 : (kMode != kChj && a.grouped) ? 1 : 2;
     int per_sm = 0;
     if (lookup)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
-    else if (!grouped)
+    else if (proj == 0)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode, kDup>, kPNT, 0));
-    else if constexpr (kDup && kMode != kChj)
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project_grouped<kMode>, kPNT, 0));
+    else
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project_grouped<kMode, false>, kPNT, 0));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
     const unsigned grid = (unsigned)std::max<uint64_t>(
         1, std::min<uint64_t>(ceil_div(std::max<uint64_t>(n_chunks, 1), kPWarps), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
     if (std::getenv("PHJ_DEBUG"))
-        std::fprintf(stderr, "[phj] %s: mode %d dup %d grid %u x %d threads, %d CTAs/SM, chunks %llu\n", name, kMode, (int)kDup, grid, kPNT, per_sm,
-                     (unsigned long long)n_chunks);
+        std::fprintf(stderr, "[phj] %s: mode %d dup %d proj %d grid %u x %d threads, %d CTAs/SM, chunks %llu\n", name, kMode, (int)kDup, proj, grid,
+                     kPNT, per_sm, (unsigned long long)n_chunks);
     // the first probe load reads an aligned pair of cells
     if ((kMode == kLeafUniform && a.uniform_log2cap < 1) || (reinterpret_cast<uintptr_t>(a.cells) & 31) != 0)
         throw Error(PHJ_ERR_CUDA, "internal: leaf tables need aligned pairs of cells");
+    if (!lookup && proj == 2)
+    {
+        KTimer kt(ctx, "probe_expand", a.probe_rows, a.probe_rows * 8 + cap * 12);
+        k_probe_expand<kMode><<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts, cap);
+        PHJ_LAUNCHED(ctx, "probe_expand");
+    }
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
+    else if (proj == 0)
+        k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
+    else if (proj == 1)
+        k_probe_project_grouped<kMode, false><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else
-    {
-        if (!grouped)
-            k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
-        else if constexpr (kDup && kMode != kChj)
-            k_probe_project_grouped<kMode><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
-    }
+        k_probe_project_grouped<kMode, true><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     PHJ_LAUNCHED(ctx, name);
 }
 
@@ -658,14 +711,27 @@ void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_
     // algorithmic bytes: the head array, the probe key and payloads of every
     // output row (read), the output rows (written)
     const uint64_t pr = row_bytes_of(a.probe, true), br = row_bytes_of(a.build, false);
-    launch_any(ctx, a, &o, const_cast<uint32_t *>(heads), const_cast<uint32_t *>(offs), rows, false, "probe_project",
-               a.probe_rows * 4 + rows * pr + rows * (8 + br + (pr - 8)));
+    ProbeArgs b = a;
+    const bool flat = a.any_dup && !(a.grouped && !a.chj);
+    if (flat)
+        b.flat = dalloc_n<uint32_t>(ctx, std::max<uint64_t>(rows, 1));
+    try
+    {
+        launch_any(ctx, b, &o, const_cast<uint32_t *>(heads), const_cast<uint32_t *>(offs), rows, false, "probe_project",
+                   a.probe_rows * 4 + rows * pr + rows * (8 + br + (pr - 8)));
+    }
+    catch (...)
+    {
+        dfree(ctx, b.flat);
+        throw;
+    }
+    dfree(ctx, b.flat);
 }
 
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, const phj_schema & left, const phj_schema & right)
 {
     ProbeArgs a = a_in;
-    if (a.grouped && !a.row_cnt)
+    if ((a.grouped || a.any_dup) && !a.row_cnt)
         a.row_cnt = s.get<uint32_t>(std::max<uint64_t>(a.probe_rows, 1));
     uint32_t * heads = s.get<uint32_t>(a.probe_rows);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(a.probe_rows) + 1);
