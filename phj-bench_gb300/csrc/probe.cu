@@ -104,35 +104,6 @@ __device__ __noinline__ uint32_t chain_length(uint32_t brow, const ProbeArgs & a
     return c;
 }
 
-template <class T>
-__device__ __forceinline__ void put(void * dst, uint64_t i, T v)
-{
-    __stcs(static_cast<T *>(dst) + i, v);
-}
-
-// One full output row (slow path for rows of duplicate-key chains).
-__device__ __forceinline__ void emit_row(const ProbeArgs & a, const OutCols & o, uint32_t brow, uint64_t key, uint64_t prow, uint64_t pos)
-{
-    __stcs(o.keys + pos, key);
-    for (uint32_t c = 0; c < a.build.n; ++c)
-        switch (a.build.width[c])
-        {
-            case 1: put<uint8_t>(o.left[c], pos, __ldg(static_cast<const uint8_t *>(a.build.col[c]) + brow)); break;
-            case 2: put<uint16_t>(o.left[c], pos, __ldg(static_cast<const uint16_t *>(a.build.col[c]) + brow)); break;
-            case 4: put<uint32_t>(o.left[c], pos, __ldg(static_cast<const uint32_t *>(a.build.col[c]) + brow)); break;
-            case 8: put<uint64_t>(o.left[c], pos, __ldg(static_cast<const uint64_t *>(a.build.col[c]) + brow)); break;
-            default: put<uint4>(o.left[c], pos, __ldg(static_cast<const uint4 *>(a.build.col[c]) + brow)); break;
-        }
-    for (uint32_t c = 0; c < a.probe.n; ++c)
-        switch (a.probe.width[c])
-        {
-            case 1: put<uint8_t>(o.right[c], pos, static_cast<const uint8_t *>(a.probe.col[c])[prow]); break;
-            case 2: put<uint16_t>(o.right[c], pos, static_cast<const uint16_t *>(a.probe.col[c])[prow]); break;
-            case 4: put<uint32_t>(o.right[c], pos, static_cast<const uint32_t *>(a.probe.col[c])[prow]); break;
-            case 8: put<uint64_t>(o.right[c], pos, static_cast<const uint64_t *>(a.probe.col[c])[prow]); break;
-            default: put<uint4>(o.right[c], pos, static_cast<const uint4 *>(a.probe.col[c])[prow]); break;
-        }
-}
 
 // Column pass of one warp over its match list: lane l writes output rows
 // base + l, base + l + 32, ... (coalesced); eight loads are in flight per
@@ -379,13 +350,11 @@ __device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t 
     }
 }
 
-// Projection: warp chunk c writes its output rows from offs[c] on.  Rows
-// with one match are written column by column; rows of duplicate keys
-// write their chains row by row.
-template <int kMode, bool kDup>
-__global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ ProbeArgs a, const __grid_constant__ OutCols o,
-                                                        const __grid_constant__ ProjCols pc, const uint32_t * __restrict__ heads,
-                                                        const uint32_t * __restrict__ offs, uint64_t out_cap)
+// Projection when no key repeats: warp chunk c writes its output rows from
+// offs[c] on, column by column.
+template <int kMode>
+__global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+                                                        const uint32_t * __restrict__ heads, const uint32_t * __restrict__ offs, uint64_t out_cap)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -405,22 +374,12 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
                 prow[k] = (uint32_t)row;
                 brow[k] = row < a.probe_rows ? __ldcs(heads + row) : kNoMatch;
             }
-            uint32_t one = 0, multi = 0;
+            uint32_t one = 0;
 #pragma unroll
             for (int k = 0; k < kPH; ++k)
             {
                 cnt[k] = brow[k] != kNoMatch ? 1u : 0u;
-                if (kDup && cnt[k])
-                {
-                    const uint64_t nx = __ldg(a.next + brow[k]);
-                    if (ref_valid(nx))
-                    {
-                        cnt[k] = chain_length(brow[k], a, kMode == kChj);
-                        multi |= 1u << k;
-                    }
-                }
-                if (cnt[k] == 1u)
-                    one |= 1u << k;
+                one |= cnt[k] << k;
             }
             // placement: warp scan per round, round-major
             uint32_t rel[kPH];
@@ -443,28 +402,11 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
             }
             // key column (the probe key), build payloads, probe payloads
             project_all(pc, brow, prow, base, rel, one);
-            if (kDup && multi)
-            {
-#pragma unroll 1
-                for (int k = 0; k < kPH; ++k)
-                    if (multi >> k & 1u)
-                    {
-                        const uint64_t key = a.probe.keys[prow[k]];
-                        uint32_t b = brow[k];
-                        for (uint64_t p = base + rel[k]; p < out_cap; ++p)
-                        {
-                            emit_row(a, o, b, key, prow[k], p);
-                            const uint64_t r = __ldg(a.next + b);
-                            if (!ref_valid(r))
-                                break;
-                            b = build_row_of<kMode>(r, a);
-                        }
-                    }
-            }
             base += running;
         }
     }
 }
+
 // Chained duplicates (CHJ, leaves too large to group, lazily built BEP
 // tables): each probe row's chain is walked once and its build rows are
 // written to a flat array at the row's output offsets, which the range
@@ -623,7 +565,7 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     if (lookup)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
     else if (proj == 0)
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode, kDup>, kPNT, 0));
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode>, kPNT, 0));
     else
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project_grouped<kMode, false>, kPNT, 0));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -645,7 +587,7 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
     else if (proj == 0)
-        k_probe_project<kMode, kDup><<<grid, kPNT, 0, ctx->stream>>>(a, *o, proj_cols(a, *o), heads, counts, cap);
+        k_probe_project<kMode><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else if (proj == 1)
         k_probe_project_grouped<kMode, false><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else
