@@ -49,9 +49,10 @@ WORKLOADS = {
            dict(kind=1, rows=1 * M, seed=0xC1, key_seed=0, types=[3]),
            dict(kind=3, rows=8 * M, seed=0xC2, key_seed=0, types=[2], domain=1 * M), [8]),
     "c3": ("PHJ-PURE multi-match 32M x 128M: ~8M distinct build keys, geometric multiplicity (mean ~4, cap 16), u8,u16,u128 "
-           "payloads; probe 50% from the distinct build keys, u32 payload; 2 passes x 8 bits", "phj-pure",
+           "payloads; probe 50% from the distinct build keys, u32 payload; radix bits, table load and first-pass tiling from "
+           "the autotuner", "phj-pure",
            dict(kind=2, rows=32 * M, seed=0xD1, key_seed=0x77, types=[0, 1, 4]),
-           dict(kind=4, rows=128 * M, seed=0xD2, key_seed=0x77, types=[2], domain=None, match_permille=500), [8, 8]),
+           dict(kind=4, rows=128 * M, seed=0xD2, key_seed=0x77, types=[2], domain=None, match_permille=500), None),
     "c4": ("PHJ (BEP) under skew 64M x 512M: unique u64 build keys with a u64 payload; probe keys Zipf(1.0) ranks through a "
            "seeded permutation onto the build keys, u32 payload; 3 passes x 6 bits; 32 MiB probe budget per CTA group "
            "(one group per SM); lazy per-leaf build", "phj",
@@ -294,6 +295,8 @@ def reference_arm(args, rank, world, dist):
     desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
     frac = args.cpu_probe_frac
+    if bits is None:
+        bits = P.autotune_radix(bspec["rows"])
     if bspec["kind"] == 2:
         bk, used = G.gen_multi_match_keys(bspec["rows"], bspec["seed"], bspec["key_seed"])
     else:
@@ -373,6 +376,11 @@ def main():
     b, p = make_tables(ctx, args.workload)
     B, Pn = b.rows, p.rows
     tuples = B + Pn
+    tuned = None
+    if bits is None:
+        import autotune
+        tuned = autotune.tune(ctx, b, p, scheme=scheme, reps=2, cache_path=None)
+        bits = tuned["pass_bits"]
     budget = args.bep_budget_mib or BEP_BUDGET_PER_GROUP.get(args.workload, 32) * ctx.get_int("num_sms")
 
     # -------- device-resident timing --------
@@ -429,7 +437,8 @@ def main():
         "config": {"workload": desc, "scheme": scheme, "build_rows": B, "probe_rows": Pn, "radix_pass_bits": bits,
                    "output_rows": out_rows,
                    "l2": f"inputs larger than L2 (probe side {Pn * row_bytes(pspec['types']) / 1e9:.1f} GB) and an L2 flush between steps",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set},
+                   "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set,
+                   "autotuned": tuned},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload),
                      "bytes_per_launch": bytes_per_launch, "ms_per_launch": avg_ms, "peak_source": peak_src},

@@ -157,6 +157,11 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *   "wait_limit_ms": bound of a device wait on another warp's work
  *        (PHJ/BEP leaf builds), 1..60000, default 1000;
  *   "host_chunk_rows": probe rows per chunk of phj_run_phj_pure_host (>= 4096);
+ *   "table_cap_pct": leaf table cells >= rows * pct / 100, rounded up to a
+ *        power of two (110..800, default 200: the reference's bit_ceil(2 rows));
+ *   "p1_tile_rows", "p1_stages": tile rows (1024/2048/4096) and bulk-copy
+ *        ring depth (2..4) of the first radix pass, 0 (default) chosen per
+ *        row width;
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
  *        leaf BUILDING before the probe, so its waits run out. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);

@@ -1031,6 +1031,10 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->host_chunk_rows = value;
     else if (std::strcmp(name, "table_cap_pct") == 0 && value >= 110 && value <= 800)
         ctx->table_cap_pct = (uint32_t)value;
+    else if (std::strcmp(name, "p1_tile_rows") == 0 && (value == 0 || value == 1024 || value == 2048 || value == 4096))
+        ctx->p1_tile_rows = (uint32_t)value;
+    else if (std::strcmp(name, "p1_stages") == 0 && (value == 0 || (value >= 2 && value <= 4)))
+        ctx->p1_stages = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
     else
@@ -1050,6 +1054,12 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->wait_limit_ms;
     else if (std::strcmp(name, "host_chunk_rows") == 0)
         *value = ctx->host_chunk_rows;
+    else if (std::strcmp(name, "table_cap_pct") == 0)
+        *value = ctx->table_cap_pct;
+    else if (std::strcmp(name, "p1_tile_rows") == 0)
+        *value = ctx->p1_tile_rows;
+    else if (std::strcmp(name, "p1_stages") == 0)
+        *value = ctx->p1_stages;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
     else if (std::strcmp(name, "device") == 0)

@@ -91,6 +91,8 @@ struct phj_ctx
     int64_t wait_limit_ms = 1000; // bound of a device wait on another warp's work
     int64_t host_chunk_rows = 16ll << 20; // probe rows per chunk of the host-buffer entry points
     uint32_t table_cap_pct = 200; // leaf table cells >= rows * pct / 100 (power of two)
+    uint32_t p1_tile_rows = 0;    // first radix pass: rows per staged tile (0: chosen per row width)
+    uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
 };
 

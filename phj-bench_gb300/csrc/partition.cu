@@ -530,6 +530,9 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
     for (int r = 8; r >= 2; r /= 2)
         for (uint32_t st = 2; st <= 4; ++st)
         {
+            // context options (an autotuner's choice) pin the tile or the depth
+            if ((ctx->p1_tile_rows && (uint32_t)(kP1NT * r) != ctx->p1_tile_rows) || (ctx->p1_stages && st != ctx->p1_stages))
+                continue;
             const uint64_t kT = (uint64_t)kP1NT * r;
             uint64_t buf = kT * 8;
             for (uint32_t c = 0; c < src.n; ++c)
