@@ -353,6 +353,7 @@ def main():
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="context option (phj_ctx_set_int)")
     ap.add_argument("--serve-requests", type=int, default=2048, help="requests of the batched/served stream (0: skip it)")
     ap.add_argument("--serve-only", action="store_true", help="run only the batched/served stream")
+    ap.add_argument("--csv", default=None, help="append the timed runs to this CSV (the reference's columns + GPU columns)")
     args = ap.parse_args()
     rank, world, local = env_rank()
     dist = Dist(world)
@@ -391,12 +392,13 @@ def main():
     sampler.start()
     dist.barrier()
     launches0 = ctx.launch_count()
-    step_ms, kernel_runs, out_rows = [], [], 0
+    step_ms, kernel_runs, out_rows, step_results = [], [], 0, []
     t_wall0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.flush_l2()
         out, res = run_scheme(ctx, scheme, b, p, bits, budget)
         step_ms.append(res.e2e_wall_ms)
+        step_results.append(res)
         kernel_runs.append(ctx.kernel_times())
         out_rows = out.rows
         if _ == args.steps - 1:
@@ -462,11 +464,12 @@ def main():
         for _ in range(2):
             out, _ = ctx.run_chj(b, p)
             out.free()
-        cms = []
+        cms, chj_results = [], []
         for _ in range(max(3, args.steps // 2)):
             ctx.flush_l2()
-            out, res = ctx.run_chj(b, p)
-            cms.append(res.e2e_wall_ms)
+            out, cres = ctx.run_chj(b, p)
+            cms.append(cres.e2e_wall_ms)
+            chj_results.append(cres)
             fp_chj = out.fingerprint()
             out.free()
         line["chj"] = {"value": tuples / (statistics.mean(cms) / 1e3), "ms_per_step": statistics.mean(cms),
@@ -526,6 +529,18 @@ def main():
                                                 budget_mib=cpu_budget_mib(args.workload, ncpu))
         except Exception as e:  # the baseline is reported, never the target
             line["cpu_baseline"] = {"value": None, "error": str(e)}
+    if args.csv and rank == 0:
+        import report
+        common = dict(threads=1, build_rows=B, probe_rows=Pn, build_types=bspec["types"], probe_types=pspec["types"],
+                      partitions=1 << sum(bits), distribution="synthetic", match_rate=pspec.get("match_permille", 1000) / 1000,
+                      gpu_device="GB300")
+        rows = [report.result_row(scheme, i, r, tuples_per_s=tuples / (r.e2e_wall_ms / 1e3), dominant_kernel=dom_name,
+                                  roofline_frac=achieved / peak, dram_gbps=bmin / (r.e2e_wall_ms / 1e3) / 1e9, **common)
+                for i, r in enumerate(step_results)]
+        if "chj" in line:
+            rows += [report.result_row("chj", i, r, tuples_per_s=tuples / (r.e2e_wall_ms / 1e3), **common)
+                     for i, r in enumerate(chj_results)]
+        report.write_csv(args.csv, rows)
     b.free(), p.free()
     ctx.close()
     # -------- batched / served request stream versus the plain form --------

@@ -245,6 +245,7 @@ struct ProbeArgs
     int grouped;
     uint32_t * row_cnt;  // per probe row: its match count (when keys repeat)
     uint32_t * flat;     // chained duplicates: build row of every output row
+    unsigned long long * out_rows64; // the lookup's 64-bit count of output rows
 };
 // PHJ/BEP lazy leaf tables.  Per probe batch: mark the leaves the batch
 // touches (one eviction per leaf and batch), queue the touched leaves still

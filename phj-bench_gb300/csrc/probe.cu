@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
     __shared__ uint16_t q_row[kPWarps * kWChunk];
     uint64_t * qkey = q_key + (threadIdx.x >> 5) * kWChunk;
     uint16_t * qrow = q_row + (threadIdx.x >> 5) * kWChunk;
+    unsigned long long grand = 0;
     for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
     {
         const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
@@ -297,7 +298,11 @@ __global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ P
             total += __shfl_xor_sync(0xffffffffu, total, o);
         if (lane == 0)
             counts[chunk] = total;
+        grand += total;
     }
+    // the join's row count in 64 bits (the chunk offsets are 32-bit)
+    if (lane == 0 && grand)
+        atomicAdd(a.out_rows64, grand);
 }
 
 // The projection walks a warp chunk in halves of kPH rounds (to bound
@@ -624,15 +629,20 @@ static uint64_t row_bytes_of(const Cols & c, bool with_key)
     return b;
 }
 
-uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, uint32_t * heads, uint32_t * counts)
+uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, uint32_t * heads, uint32_t * counts)
 {
-    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_chunks = ceil_div(a_in.probe_rows, kWChunk);
+    ProbeArgs a = a_in;
+    a.out_rows64 = s.get<unsigned long long>(1);
+    PHJ_CUDA(cudaMemsetAsync(a.out_rows64, 0, sizeof(unsigned long long), ctx->stream));
     // algorithmic bytes: probe keys read, head array written
     launch_any(ctx, a, nullptr, heads, counts, 0, true, "probe_lookup", a.probe_rows * (8 + 4));
     scan_u32(ctx, s, counts, counts, n_chunks);
-    uint32_t total = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&total, counts + n_chunks, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long total = 0;
+    PHJ_CUDA(cudaMemcpyAsync(&total, a.out_rows64, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
     PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (total >= (1ull << 32))
+        throw Error(PHJ_ERR_CAPACITY, "the join has " + std::to_string(total) + " output rows; the device schemes place at most 2^32 - 1");
     return total;
 }
 
