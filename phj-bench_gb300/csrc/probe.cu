@@ -332,7 +332,10 @@ __device__ __forceinline__ void project_column(const void * src_v, void * dst_v,
             __stcs(dst + rel[u], v[u]);
 }
 
-// All output columns, one switch instance for the loop.
+// All output columns, one switch instance for the loop.  Without 16-byte
+// columns (kWide false) the widest staged value is 8 bytes, which keeps the
+// plain projection at four CTAs per SM.
+template <bool kWide = true>
 __device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t (&brow)[kPH], const uint32_t (&prow)[kPH], uint64_t base,
                                             const uint32_t (&rel)[kPH], uint32_t one)
 {
@@ -350,15 +353,18 @@ __device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t 
             case 2: project_column<uint16_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
             case 4: project_column<uint32_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
             case 8: project_column<uint64_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
-            default: project_column<uint4>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            default:
+                if constexpr (kWide)
+                    project_column<uint4>(pc.src[c], pc.dst[c], idx, base, rel, one, g);
+                break;
         }
     }
 }
 
 // Projection when no key repeats: warp chunk c writes its output rows from
 // offs[c] on, column by column.
-template <int kMode>
-__global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+template <int kMode, bool kWide>
+__global__ void __launch_bounds__(kPNT, kWide ? 1 : 4) k_probe_project(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
                                                         const uint32_t * __restrict__ heads, const uint32_t * __restrict__ offs, uint64_t out_cap)
 {
     const uint32_t lane = threadIdx.x & 31;
@@ -406,7 +412,7 @@ __global__ void __launch_bounds__(kPNT) k_probe_project(const __grid_constant__ 
                     one &= ~(1u << k);
             }
             // key column (the probe key), build payloads, probe payloads
-            project_all(pc, brow, prow, base, rel, one);
+            project_all<kWide>(pc, brow, prow, base, rel, one);
             base += running;
         }
     }
@@ -566,11 +572,16 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     // projection: plain (no repeated keys), range (grouped leaves) or flat
     // (chains expanded first)
     const int proj = !kDup ? 0 : (kMode != kChj && a.grouped) ? 1 : 2;
+    bool wide = false; // a 16-byte payload column
+    for (uint32_t c = 0; c < a.build.n; ++c)
+        wide = wide || a.build.width[c] > 8;
+    for (uint32_t c = 0; c < a.probe.n; ++c)
+        wide = wide || a.probe.width[c] > 8;
     int per_sm = 0;
     if (lookup)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
     else if (proj == 0)
-        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project<kMode>, kPNT, 0));
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide ? k_probe_project<kMode, true> : k_probe_project<kMode, false>, kPNT, 0));
     else
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_probe_project_grouped<kMode, false>, kPNT, 0));
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
@@ -591,8 +602,10 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
+    else if (proj == 0 && wide)
+        k_probe_project<kMode, true><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else if (proj == 0)
-        k_probe_project<kMode><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
+        k_probe_project<kMode, false><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else if (proj == 1)
         k_probe_project_grouped<kMode, false><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else
