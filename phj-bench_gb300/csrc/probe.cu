@@ -146,7 +146,7 @@ __device__ __forceinline__ void columns_pass(const Cols & src, void * const * ds
 // Lookups: per probe row its head build row (kNoMatch when the key is
 // absent), per warp chunk its number of output rows.
 template <int kMode, bool kDup>
-__global__ void __launch_bounds__(kPNT) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
+__global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
                                                        uint32_t * __restrict__ counts)
 {
     const uint32_t lane = threadIdx.x & 31;
