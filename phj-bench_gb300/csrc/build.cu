@@ -52,7 +52,8 @@ __device__ __forceinline__ uint32_t log2u(uint64_t x)
 // leaf << ulog, ulog >= 0) or sized per leaf through table_off (ulog < 0).
 // The RowRefCell of a build row is {0, row}: block 0 is the whole
 // leaf-partitioned build side, row its index there.
-__global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __restrict__ keys, const uint32_t * __restrict__ leaf_off,
+template <int NT>
+__global__ void __launch_bounds__(NT) k_build_leaf(const uint64_t * __restrict__ keys, const uint32_t * __restrict__ leaf_off,
                                                          const uint32_t * __restrict__ table_off, int ulog, uint32_t smem_cells,
                                                          Cell * __restrict__ cells, uint64_t * __restrict__ next, LeafMeta * __restrict__ meta,
                                                          int * __restrict__ any_dup)
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
     const Cell empty{0ull, INVALID_REF};
     if (r == 0)
     {
-        for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT) // uniform layout: an empty table
+        for (uint64_t i = threadIdx.x; i < cap; i += NT) // uniform layout: an empty table
             reinterpret_cast<ulonglong2 *>(cells + t0)[i] = make_ulonglong2(0ull, INVALID_REF);
         if (threadIdx.x == 0)
             meta[l] = LeafMeta{t0, r0, cap ? (uint8_t)log2u(cap) : (uint8_t)0, 0, 0, 0};
@@ -76,11 +77,11 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
     }
     const bool in_smem = cap <= smem_cells;
     Cell * tab = in_smem ? sh_cells : cells + t0;
-    for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT)
+    for (uint64_t i = threadIdx.x; i < cap; i += NT)
         tab[i] = empty;
     __syncthreads();
     bool my_dup = false;
-    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+    for (uint32_t i = threadIdx.x; i < r; i += NT)
     {
         const uint64_t k = keys[r0 + i];
         const uint64_t h = int_hash64(k);
@@ -96,7 +97,7 @@ __global__ void __launch_bounds__(kBuildNT) k_build_leaf(const uint64_t * __rest
     {
         ulonglong2 * dst = reinterpret_cast<ulonglong2 *>(cells + t0);
         const ulonglong2 * src = reinterpret_cast<const ulonglong2 *>(sh_cells);
-        for (uint64_t i = threadIdx.x; i < cap; i += kBuildNT)
+        for (uint64_t i = threadIdx.x; i < cap; i += NT)
             dst[i] = src[i];
     }
     if (threadIdx.x == 0)
@@ -271,7 +272,8 @@ __global__ void k_chj_insert(const uint64_t * __restrict__ keys, uint64_t n, uin
 void set_build_smem_limits(int smem_optin)
 {
     const size_t need = (size_t)kSmemCellsMax * sizeof(Cell);
-    PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
+    PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf<kBuildNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
+    PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
     PHJ_CUDA(cudaFuncSetAttribute(k_group_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::min<size_t>((size_t)kSmemCellsMax * 12, (size_t)smem_optin - 1024)));
 }
@@ -345,7 +347,10 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     int * any_dup = reinterpret_cast<int *>(small + 1);
     {
         KTimer kt(ctx, "build_leaf_tables", 0, 0);
-        k_build_leaf<<<n_leaves, kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, lt.uniform_log2cap,
+        // leaves of more than 1024 rows (few, large leaves: one resident CTA
+        // per SM by shared memory) get 1024 threads
+        auto kb = lt.max_rows > 1024 ? k_build_leaf<1024> : k_build_leaf<kBuildNT>;
+        kb<<<n_leaves, lt.max_rows > 1024 ? 1024 : kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, lt.uniform_log2cap,
                                                                                             smem_cells, lt.cells, lt.next, lt.meta, any_dup);
         PHJ_LAUNCHED(ctx, "build_leaf");
     }
