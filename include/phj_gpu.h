@@ -301,6 +301,7 @@ typedef struct phj_serve_record {
     uint32_t batch_size;           /* joins in the launch set that ran it (1: alone) */
     uint32_t slot;
     int32_t status;                /* phj_status; -1 while not done */
+    uint64_t job_peak_bytes;       /* measured peak device bytes of the launch set (inputs included) */
 } phj_serve_record;
 
 typedef struct phj_server phj_server;

@@ -119,6 +119,7 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
         else
             s = phj_batch_run(ctx, (uint32_t)n, b.data(), p.data(), o.data(), nullptr);
     }
+    const uint64_t job_peak = ctx->peak_bytes; // the scheme run's peak, inputs and outputs included
     for (size_t i = 0; i < n; ++i)
     {
         if (s == PHJ_OK && o[i])
@@ -143,6 +144,7 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
         for (int k = 0; k < 3; ++k)
             r.fingerprint[k] = fp[i][k];
         r.output_rows = fp[i][0];
+        r.job_peak_bytes = job_peak;
         S.inflight_bytes -= S.footprint[job[i]];
         S.inflight_requests -= 1;
         ++S.completed;

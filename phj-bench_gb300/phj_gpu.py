@@ -107,7 +107,7 @@ class ServeRecord(C.Structure):
     _fields_ = [("id", C.c_uint64), ("arrival_s", C.c_double), ("admit_s", C.c_double), ("start_s", C.c_double),
                 ("done_s", C.c_double), ("build_rows", C.c_uint64), ("probe_rows", C.c_uint64), ("output_rows", C.c_uint64),
                 ("footprint_bytes", C.c_uint64), ("fingerprint", C.c_uint64 * 3), ("batch_size", C.c_uint32), ("slot", C.c_uint32),
-                ("status", C.c_int32)]
+                ("status", C.c_int32), ("job_peak_bytes", C.c_uint64)]
 
 
 _lib = None
@@ -614,7 +614,7 @@ class Server:
         return [{"id": r.id, "arrival_s": r.arrival_s, "admit_s": r.admit_s, "start_s": r.start_s, "done_s": r.done_s,
                  "build_rows": r.build_rows, "probe_rows": r.probe_rows, "output_rows": r.output_rows,
                  "footprint_bytes": r.footprint_bytes, "fingerprint": tuple(r.fingerprint), "batch_size": r.batch_size,
-                 "slot": r.slot, "status": r.status} for r in arr[:n]]
+                 "slot": r.slot, "status": r.status, "job_peak_bytes": r.job_peak_bytes} for r in arr[:n]]
 
     def close(self):
         if self.ptr:

@@ -108,6 +108,10 @@ def test_served_results_equal_alone(ctx, mode):
         assert len({r["slot"] for r in recs}) > 1
     else:
         assert all(r["batch_size"] == 1 for r in recs)
+        # the admission estimate bounds the measured device footprint of a
+        # join run alone (inputs, partitions, tables, output)
+        for r in recs:
+            assert 0 < r["job_peak_bytes"] <= r["footprint_bytes"] * 1.05 + (8 << 20), r
 
 
 def test_served_small_requests_match_oracle():
