@@ -651,7 +651,11 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             peak_rows = std::max(peak_rows, n_b);
             Scratch sb(ctx);
             PHJ_CUDA(cudaEventRecord(eb[0], ctx->stream));
+            // the batch's first radix pass also flags the leaves its rows
+            // touch (its histogram reads every key once anyway)
+            ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
             radix_partition(ctx, sb, cols_from(pin, r0), n_b, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            ctx->leaf_mark = LeafMark{};
             k_count_nonempty<<<(unsigned)ceil_div(p1, 256), 256, 0, ctx->stream>>>(poff, p1, ctr + 3);
             PHJ_LAUNCHED(ctx, "count_refinements");
             PHJ_CUDA(cudaEventRecord(eb[1], ctx->stream));
@@ -659,7 +663,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             a.probe_rows = n_b;
             // lazy build of the leaves this batch touches
             PHJ_CUDA(cudaEventRecord(eb[3], ctx->stream));
-            a.any_dup = bep_build_touched(ctx, bl, ppart.keys, n_b) ? 1 : 0;
+            a.any_dup = bep_build_touched(ctx, bl) ? 1 : 0;
             check_device_error(ctx);
             PHJ_CUDA(cudaEventRecord(eb[4], ctx->stream));
             const uint64_t rows = probe_lookup(ctx, sb, a, heads, counts);

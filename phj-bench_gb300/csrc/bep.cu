@@ -1,9 +1,9 @@
 // bep.cu -- lazy leaf tables of the PHJ (BEP) scheme: each leaf table is
 // built the first time a probe batch needs it.
 //
-// Per batch, before its lookups: k_bep_mark hashes the batch's probe keys
-// and flags the leaves they touch; k_bep_collect counts each touched leaf
-// as one eviction (its buffered rows are probed in this batch) and queues
+// Per batch, before its lookups: the batch's first radix pass (its
+// histogram kernel) flags the leaves the probe keys touch in a bitmap;
+// k_bep_collect counts each touched leaf as one eviction (its buffered rows are probed in this batch) and queues
 // the touched leaves that are not yet built.  k_bep_build is a persistent
 // grid whose CTAs take leaves from that queue: a CTA wins NOT_BUILT ->
 // BUILDING with a CAS, builds the table in shared memory with 128-bit CAS
@@ -20,8 +20,6 @@ namespace
 constexpr uint32_t kNotBuilt = 0, kBuilding = 1, kBuilt = 2, kBuiltDup = 3;
 constexpr int kBepNT = 256;
 constexpr uint32_t kBepSmemCellsMax = 8192; // 128 KiB of cells per CTA
-constexpr int kMarkNT = 512;
-constexpr size_t kBepMaxMarkLeaves = 1u << 20; // the CTA bitmap (128 KiB) bounds the leaf count
 
 __device__ __forceinline__ uint32_t load_acquire(const uint32_t * p)
 {
@@ -35,39 +33,6 @@ __device__ __forceinline__ uint64_t global_ns()
     uint64_t t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
-}
-
-// Marks the leaves a batch's probe keys touch in a bitmap.  Each CTA sets
-// bits of its own shared-memory copy (a bit is read before it is set, so
-// the hot leaves of a skewed probe side cost a shared-memory read) and ORs
-// the copy into the global bitmap at the end.
-__global__ void __launch_bounds__(kMarkNT) k_bep_mark(BepLeaves b, const uint64_t * __restrict__ keys, uint64_t n)
-{
-    extern __shared__ uint32_t bm[];
-    const uint32_t words = (b.n_leaves + 31) / 32;
-    for (uint32_t w = threadIdx.x; w < words; w += kMarkNT)
-        bm[w] = 0;
-    __syncthreads();
-    const uint32_t shift = 64u - b.leaf_bits;
-    const uint64_t stride = (uint64_t)gridDim.x * kMarkNT;
-    for (uint64_t i = (uint64_t)blockIdx.x * kMarkNT + threadIdx.x; i < n; i += 4 * stride)
-    {
-        uint32_t L[4];
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-        {
-            const uint64_t r = i + u * stride;
-            L[u] = r < n ? (uint32_t)(int_hash64(__ldcs(keys + r)) >> shift) : 0xFFFFFFFFu;
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u)
-            if (L[u] != 0xFFFFFFFFu && !(bm[L[u] >> 5] & (1u << (L[u] & 31))))
-                atomicOr(&bm[L[u] >> 5], 1u << (L[u] & 31));
-    }
-    __syncthreads();
-    for (uint32_t w = threadIdx.x; w < words; w += kMarkNT)
-        if (bm[w])
-            atomicOr(b.touched + w, bm[w]);
 }
 
 // One pass over the leaves, a warp per bitmap word: each touched leaf is one
@@ -181,22 +146,13 @@ __global__ void __launch_bounds__(kBepNT) k_bep_build(BepLeaves b, int * __restr
 
 void set_bep_smem_limits(int smem_optin)
 {
-    PHJ_CUDA(cudaFuncSetAttribute(k_bep_mark, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(kBepMaxMarkLeaves / 8, (size_t)smem_optin - 1024)));
     PHJ_CUDA(cudaFuncSetAttribute(k_bep_build, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::min<size_t>((size_t)kBepSmemCellsMax * sizeof(Cell), (size_t)smem_optin - 1024)));
 }
 
-bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b, const uint64_t * probe_keys, uint64_t n)
+bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b)
 {
     PHJ_CUDA(cudaMemsetAsync(b.queue_len, 0, 2 * sizeof(uint32_t), ctx->stream));
-    if (n)
-    {
-        KTimer kt(ctx, "bep_mark", n, n * 8);
-        const size_t bm_bytes = (size_t)((b.n_leaves + 31) / 32) * 4;
-        const unsigned grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(n, kMarkNT * 16), (uint64_t)ctx->num_sms * 2));
-        k_bep_mark<<<grid, kMarkNT, bm_bytes, ctx->stream>>>(b, probe_keys, n);
-        PHJ_LAUNCHED(ctx, "bep_mark");
-    }
     k_bep_collect<<<(unsigned)ceil_div(b.n_leaves, kBepNT), kBepNT, 0, ctx->stream>>>(b);
     PHJ_LAUNCHED(ctx, "bep_collect");
     {

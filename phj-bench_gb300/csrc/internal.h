@@ -63,6 +63,15 @@ inline uint64_t schema_bytes(const phj_schema & s)
 }
 } // namespace phjg
 
+// A request to flag leaves during the next first radix pass (PHJ/BEP
+// batches): bit (hash >> shift) of `bits` (`words` 32-bit words).
+struct LeafMark
+{
+    uint32_t * bits = nullptr;
+    uint32_t shift = 0;
+    uint32_t words = 0;
+};
+
 struct phj_ctx
 {
     int device = 0;
@@ -94,6 +103,7 @@ struct phj_ctx
     uint32_t p1_tile_rows = 0;    // first radix pass: rows per staged tile (0: chosen per row width)
     uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
+    LeafMark leaf_mark;           // consumed by the next first radix pass
 };
 
 struct phj_table
@@ -247,12 +257,12 @@ struct ProbeArgs
     uint32_t * flat;     // chained duplicates: build row of every output row
     unsigned long long * out_rows64; // the lookup's 64-bit count of output rows
 };
-// PHJ/BEP lazy leaf tables.  Per probe batch: mark the leaves the batch
-// touches (one eviction per leaf and batch), queue the touched leaves still
-// NOT_BUILT, and let persistent warps take leaves from that queue and build
-// them (NOT_BUILT -> BUILDING -> BUILT; a leaf found BUILDING is waited for,
-// bounded by wait_limit_ns).  Counters: [0] tables built, [1] waits on a
-// BUILDING leaf, [2] evictions.
+// PHJ/BEP lazy leaf tables.  Per probe batch: the leaves the batch touches
+// are flagged (one eviction per leaf and batch), the touched leaves still
+// NOT_BUILT are queued, and persistent CTAs take leaves from that queue and
+// build them (NOT_BUILT -> BUILDING -> BUILT; a leaf found BUILDING is
+// waited for, bounded by wait_limit_ns).  Counters: [0] tables built, [1]
+// waits on a BUILDING leaf, [2] evictions.
 struct BepLeaves
 {
     uint32_t * state;             // per leaf: 0 NOT_BUILT, 1 BUILDING, 2 BUILT, 3 BUILT (keys repeat)
@@ -273,7 +283,9 @@ struct BepLeaves
 };
 // Builds the leaves the batch's probe keys touch.  Returns whether any leaf
 // built so far has a repeated key (the lookup then follows chains).
-bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b, const uint64_t * probe_keys, uint64_t n);
+// The batch's leaves are flagged in b.touched by its first radix pass
+// (ctx->leaf_mark) before this runs.
+bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b);
 void set_bep_smem_limits(int smem_optin);
 
 // Lookups, then an exactly sized output, then the projection.

@@ -244,13 +244,20 @@ struct P1Geom
 // H CTAs share one scatter CTA's row range (counts are zeroed first and
 // summed with global atomics), so the histogram keeps more loads in flight
 // than the scatter's one-CTA-per-SM grid would.
+// With `mark` set (PHJ/BEP probe batches) the same pass also flags the
+// leaves the rows hash to: a shared-memory bitmap per CTA (a bit is read
+// before it is set), ORed into the global bitmap at the end.
 __global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__ keys, P1Geom g, uint32_t H, uint32_t G,
-                                                   uint32_t * __restrict__ counts)
+                                                   uint32_t * __restrict__ counts, LeafMark mark)
 {
     extern __shared__ uint32_t bins[];
     const uint32_t nb = 1u << g.b, mask = nb - 1;
+    uint32_t * bm = bins + nb;
     for (uint32_t i = threadIdx.x; i < nb; i += kP1NT)
         bins[i] = 0;
+    if (mark.bits)
+        for (uint32_t i = threadIdx.x; i < mark.words; i += kP1NT)
+            bm[i] = 0;
     __syncthreads();
     const uint32_t gi = blockIdx.x / H, q = blockIdx.x % H;
     const uint64_t span = (uint64_t)g.tiles_per_cta * g.tile_rows;
@@ -271,12 +278,28 @@ __global__ void __launch_bounds__(kP1NT) k_p1_hist(const uint64_t * __restrict__
 #pragma unroll
         for (int j = 0; j < 8; ++j)
             if (base + j * kP1NT + threadIdx.x < r1)
-                atomicAdd(&bins[(uint32_t)(int_hash64(k[j]) >> g.shift) & mask], 1u);
+            {
+                const uint64_t h = int_hash64(k[j]);
+                atomicAdd(&bins[(uint32_t)(h >> g.shift) & mask], 1u);
+                if (mark.bits)
+                {
+                    const uint32_t L = (uint32_t)(h >> mark.shift);
+                    if (!(bm[L >> 5] & (1u << (L & 31))))
+                        atomicOr(&bm[L >> 5], 1u << (L & 31));
+                }
+            }
     }
     __syncthreads();
     for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
         if (bins[d])
             atomicAdd(&counts[(uint64_t)d * G + gi], bins[d]);
+    if (mark.bits)
+        for (uint32_t w = threadIdx.x; w < mark.words; w += kP1NT)
+        {
+            const uint32_t v = bm[w];
+            if (v && (__ldcg(mark.bits + w) & v) != v)
+                atomicOr(mark.bits + w, v);
+        }
 }
 
 struct P1Smem
@@ -578,7 +601,10 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
     {
         const uint32_t H = 4;
         KTimer kt(ctx, "part_hist", n, n * 8);
-        k_p1_hist<<<G * H, kP1NT, nb * sizeof(uint32_t), ctx->stream>>>(src.keys, g, H, G, counts);
+        // a pending leaf mark (PHJ/BEP) rides on this pass, once
+        const LeafMark mark = ctx->leaf_mark;
+        ctx->leaf_mark = LeafMark{};
+        k_p1_hist<<<G * H, kP1NT, (size_t)(nb + (mark.bits ? mark.words : 0)) * sizeof(uint32_t), ctx->stream>>>(src.keys, g, H, G, counts, mark);
         PHJ_LAUNCHED(ctx, "p1_hist");
     }
     scan_u32(ctx, s, counts, counts, (uint64_t)nb * G);
@@ -680,6 +706,8 @@ void set_partition_smem_limits(int smem_optin)
 {
     PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
     PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)std::min<size_t>(((1u << kMaxPassBits) + (1u << 20) / 32) * sizeof(uint32_t), (size_t)smem_optin - 1024)));
     PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
     // The scatter kernel stages a 4096-row tile of the widest column (<= 16
     // bytes) plus digit bins: up to ~96 KiB.
