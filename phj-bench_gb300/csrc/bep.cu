@@ -69,73 +69,101 @@ __global__ void k_bep_collect(BepLeaves b)
 // shared memory (or in place when it is larger than `smem_cells`), copies it
 // out, threads the next-chain and publishes BUILT; or it finds the leaf
 // BUILDING and waits for it (bounded).
+// Leaves a CTA claims from the queue at once: their NOT_BUILT -> BUILDING
+// CASes and, after the builds, their BUILT stores run in parallel, so the
+// per-leaf cost is the build itself rather than a chain of global round
+// trips.
+constexpr uint32_t kClaim = 8;
+
 __global__ void __launch_bounds__(kBepNT) k_bep_build(BepLeaves b, int * __restrict__ err)
 {
     extern __shared__ __align__(16) Cell sh_cells[];
-    __shared__ uint32_t s_leaf, s_won, s_stop;
+    __shared__ uint32_t s_leaf[kClaim], s_won[kClaim], s_dup[kClaim];
+    __shared__ uint32_t s_n, s_stop;
     for (;;)
     {
         if (threadIdx.x == 0)
         {
-            const uint32_t idx = atomicAdd(b.queue_len + 1, 1u);
-            s_leaf = idx < *reinterpret_cast<volatile uint32_t *>(b.queue_len) ? b.queue[idx] : 0xFFFFFFFFu;
-            s_won = s_leaf != 0xFFFFFFFFu && atomicCAS(b.state + s_leaf, kNotBuilt, kBuilding) == kNotBuilt;
+            const uint32_t base = atomicAdd(b.queue_len + 1, kClaim);
+            const uint32_t qlen = *reinterpret_cast<volatile uint32_t *>(b.queue_len);
+            s_n = base < qlen ? min(kClaim, qlen - base) : 0u;
             s_stop = 0;
+            s_leaf[0] = base; // read below by the claiming threads
         }
         __syncthreads();
-        const uint32_t L = s_leaf;
-        if (L == 0xFFFFFFFFu)
+        const uint32_t n = s_n;
+        if (n == 0)
             return;
-        if (s_won)
+        const uint32_t base = s_leaf[0];
+        __syncthreads();
+        if (threadIdx.x < n)
         {
-            const LeafMeta m = b.meta[L];
-            bool dup = false;
-            if (m.has_table)
+            const uint32_t L = b.queue[base + threadIdx.x];
+            s_leaf[threadIdx.x] = L;
+            s_won[threadIdx.x] = atomicCAS(b.state + L, kNotBuilt, kBuilding) == kNotBuilt;
+            s_dup[threadIdx.x] = 0;
+        }
+        __syncthreads();
+        for (uint32_t i = 0; i < n; ++i)
+        {
+            const uint32_t L = s_leaf[i];
+            if (s_won[i])
             {
-                const uint64_t cap = 1ull << m.log2cap;
-                const bool in_smem = cap <= b.smem_cells;
-                Cell * tab = in_smem ? sh_cells : b.cells + m.table_off;
-                for (uint64_t i = threadIdx.x; i < cap; i += kBepNT)
-                    reinterpret_cast<ulonglong2 *>(tab)[i] = make_ulonglong2(0ull, INVALID_REF);
-                __syncthreads();
-                const uint32_t r0 = m.row_off, r1 = b.leaf_off[L + 1];
-                for (uint32_t r = r0 + threadIdx.x; r < r1; r += kBepNT)
+                const LeafMeta m = b.meta[L];
+                bool dup = false;
+                if (m.has_table)
                 {
-                    const uint64_t k = b.build_keys[r];
-                    const uint64_t h = int_hash64(k);
-                    const uint64_t prev = in_smem ? table_insert<true>(tab, cap, h, k, make_ref(0, r)) : table_insert<false>(tab, cap, h, k, make_ref(0, r));
-                    b.next[r] = prev;
-                    dup |= ref_valid(prev);
+                    const uint64_t cap = 1ull << m.log2cap;
+                    const bool in_smem = cap <= b.smem_cells;
+                    Cell * tab = in_smem ? sh_cells : b.cells + m.table_off;
+                    for (uint64_t j = threadIdx.x; j < cap; j += kBepNT)
+                        reinterpret_cast<ulonglong2 *>(tab)[j] = make_ulonglong2(0ull, INVALID_REF);
+                    __syncthreads();
+                    const uint32_t r0 = m.row_off, r1 = b.leaf_off[L + 1];
+                    for (uint32_t r = r0 + threadIdx.x; r < r1; r += kBepNT)
+                    {
+                        const uint64_t k = b.build_keys[r];
+                        const uint64_t h = int_hash64(k);
+                        const uint64_t prev =
+                            in_smem ? table_insert<true>(tab, cap, h, k, make_ref(0, r)) : table_insert<false>(tab, cap, h, k, make_ref(0, r));
+                        b.next[r] = prev;
+                        dup |= ref_valid(prev);
+                    }
+                    dup = __syncthreads_or(dup);
+                    if (in_smem)
+                        for (uint64_t j = threadIdx.x; j < cap; j += kBepNT)
+                            reinterpret_cast<ulonglong2 *>(b.cells + m.table_off)[j] = reinterpret_cast<const ulonglong2 *>(sh_cells)[j];
                 }
-                dup = __syncthreads_or(dup);
-                if (in_smem)
-                    for (uint64_t i = threadIdx.x; i < cap; i += kBepNT)
-                        reinterpret_cast<ulonglong2 *>(b.cells + m.table_off)[i] = reinterpret_cast<const ulonglong2 *>(sh_cells)[i];
+                if (threadIdx.x == 0)
+                    s_dup[i] = dup;
+                __syncthreads(); // the shared table is reused by the next leaf
             }
-            // the tables are read by the lookups of a later kernel, so
-            // BUILT needs no fence for them; it only releases waiters
-            __syncthreads();
-            if (threadIdx.x == 0)
+            else if (threadIdx.x == 0 && load_acquire(b.state + L) < kBuilt)
             {
-                b.meta[L].dup = dup ? 1 : 0;
-                atomicExch(b.state + L, dup ? kBuiltDup : kBuilt);
-                atomicAdd(b.ctr + 0, 1ull);
-                if (dup)
-                    atomicExch(b.any_dup, 1);
+                atomicAdd(b.ctr + 1, 1ull);
+                const uint64_t t0 = global_ns();
+                uint32_t spins = 0;
+                while (load_acquire(b.state + L) < kBuilt)
+                    if (++spins >= kWaitLimit || global_ns() - t0 > b.wait_limit_ns)
+                    {
+                        atomicExch(err, 4);
+                        s_stop = 1;
+                        break;
+                    }
             }
         }
-        else if (threadIdx.x == 0 && load_acquire(b.state + L) < kBuilt)
+        __syncthreads();
+        // the tables are read by the lookups of a later kernel, so BUILT
+        // needs no fence for them; it only releases waiters
+        if (threadIdx.x < n && s_won[threadIdx.x])
         {
-            atomicAdd(b.ctr + 1, 1ull);
-            const uint64_t t0 = global_ns();
-            uint32_t spins = 0;
-            while (load_acquire(b.state + L) < kBuilt)
-                if (++spins >= kWaitLimit || global_ns() - t0 > b.wait_limit_ns)
-                {
-                    atomicExch(err, 4);
-                    s_stop = 1;
-                    break;
-                }
+            const uint32_t L = s_leaf[threadIdx.x];
+            const bool dup = s_dup[threadIdx.x] != 0;
+            b.meta[L].dup = dup ? 1 : 0;
+            atomicExch(b.state + L, dup ? kBuiltDup : kBuilt);
+            atomicAdd(b.ctr + 0, 1ull);
+            if (dup)
+                atomicExch(b.any_dup, 1);
         }
         __syncthreads();
         if (s_stop)
