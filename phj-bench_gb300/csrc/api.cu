@@ -740,7 +740,11 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     const uint32_t n_leaves = 1u << total_bits;
     const uint64_t B_rows = hb.total_rows, P_rows = hp.total_rows;
     const uint64_t C = std::max<uint64_t>(1, std::min<uint64_t>(chunk_rows, std::max<uint64_t>(P_rows, 1)));
-    const uint64_t n_chunks = ceil_div(P_rows, C);
+    // chunk c covers rows [start(c), start(c + 1)): the first chunk is a
+    // quarter of the others, so the first output download starts sooner
+    const uint64_t C0 = std::max<uint64_t>(1, std::min<uint64_t>(C, std::max<uint64_t>(C / 4, 4096)));
+    auto start = [&](uint64_t c) -> uint64_t { return c == 0 ? 0 : std::min(P_rows, C0 + (c - 1) * C); };
+    const uint64_t n_chunks = P_rows == 0 ? 0 : (P_rows <= C0 ? 1 : 1 + ceil_div(P_rows - C0, C));
     cudaEvent_t ev[4];
     for (auto & e : ev)
         e = take_event(ctx);
@@ -782,7 +786,7 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     auto enqueue_chunk = [&](uint64_t c) {
         if (c >= 2)
             PHJ_CUDA(cudaStreamWaitEvent(ctx->h2d, used[c - 2], 0));
-        upload(in[c & 1], hp, c * C, std::min(C, P_rows - c * C));
+        upload(in[c & 1], hp, start(c), start(c + 1) - start(c));
         PHJ_CUDA(cudaEventRecord(up[c], ctx->h2d));
     };
     for (uint64_t c = 0; c < std::min<uint64_t>(2, n_chunks); ++c)
@@ -826,7 +830,7 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     {
         for (uint64_t c = 0; c < n_chunks; ++c)
         {
-            const uint64_t n = std::min(C, P_rows - c * C);
+            const uint64_t n = start(c + 1) - start(c);
             Scratch sc(ctx);
             PHJ_CUDA(cudaStreamWaitEvent(S, up[c], 0));
             PHJ_CUDA(cudaEventRecord(c0, S));
