@@ -328,7 +328,6 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
     constexpr uint32_t kMaxStages = 4;
     extern __shared__ __align__(16) uint8_t smem[];
     __shared__ __align__(8) uint64_t bar[kMaxStages];
-    __shared__ uint32_t ws[kP1NT / 32];
     uint16_t * inv = reinterpret_cast<uint16_t *>(smem + (size_t)stages * sm.buf_bytes);
     uint16_t * dsort = inv + kT;
     const uint32_t nb = 1u << g.b, mask = nb - 1;
@@ -342,7 +341,10 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
     if (t_begin >= t_end)
         return;
     for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+    {
         cursor[d] = offs[(uint64_t)d * gridDim.x + blockIdx.x];
+        bins[d] = 0;
+    }
     if (threadIdx.x == 0)
     {
         for (uint32_t i = 0; i < stages; ++i)
@@ -403,15 +405,14 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
             for (uint32_t c = 0; c < in.n; ++c)
                 for (uint32_t i = threadIdx.x; i < cnt; i += kP1NT)
                     copy_elem(buf + sm.col_off[c], i, in.col[c], t * kT + i, in.width[c]);
+            __syncthreads();
         }
         // keep stages-1 tiles in flight: refill the buffer the previous tile
         // used (its readers finished at the barrier ending that iteration)
         const uint32_t nbi = (bi + stages - 1) % stages;
         if (threadIdx.x == 0 && t + stages - 1 < t_end && tma_ok(t + stages - 1))
             issue(t + stages - 1, nbi);
-        for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
-            bins[d] = 0;
-        __syncthreads();
+        // (bins were zeroed with the cursor update that ended the last tile)
 
         const uint64_t * bk = reinterpret_cast<const uint64_t *>(buf);
         uint32_t dg[RPT], rk[RPT];
@@ -428,15 +429,26 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
             }
         }
         __syncthreads();
+        // exclusive scan of the digit counts by the first warp alone: one
+        // barrier instead of the block scan's three
+        if (threadIdx.x < 32)
         {
-            const uint32_t per = (nb + kP1NT - 1) / kP1NT;
-            const uint32_t b0 = threadIdx.x * per;
+            const uint32_t lane = threadIdx.x;
+            const uint32_t per = (nb + 31) / 32;
+            const uint32_t b0 = lane * per;
             uint32_t local = 0;
             for (uint32_t i = 0; i < per; ++i)
                 if (b0 + i < nb)
                     local += bins[b0 + i];
-            uint32_t total;
-            uint32_t run = block_excl_scan<kP1NT>(local, ws, &total);
+            uint32_t x = local;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= (uint32_t)d)
+                    x += y;
+            }
+            uint32_t run = x - local;
             for (uint32_t i = 0; i < per; ++i)
                 if (b0 + i < nb)
                 {
@@ -483,7 +495,10 @@ __global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__
         }
         __syncthreads(); // cursor/bins reuse; this buffer is refilled next iteration
         for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
+        {
             cursor[d] += bins[d];
+            bins[d] = 0; // for the next tile's ranks
+        }
     }
     // Bulk copies still in flight (only after a timeout) must land before
     // the CTA's shared memory is released.
