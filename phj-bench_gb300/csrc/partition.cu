@@ -93,16 +93,28 @@ __global__ void __launch_bounds__(kNT) k_part_hist(const uint64_t * __restrict__
 }
 
 // Exclusive scan of nb bins in shared memory by kNT threads.
-__device__ __forceinline__ void smem_bins_scan(const uint32_t * bins, uint32_t * excl, uint32_t nb, uint32_t * ws)
+// Exclusive scan of the tile's digit counts by the first warp alone (the
+// caller's next barrier publishes excl).
+__device__ __forceinline__ void smem_bins_scan(const uint32_t * bins, uint32_t * excl, uint32_t nb)
 {
-    const uint32_t per = (nb + kNT - 1) / kNT;
-    const uint32_t b0 = threadIdx.x * per;
+    if (threadIdx.x >= 32)
+        return;
+    const uint32_t lane = threadIdx.x;
+    const uint32_t per = (nb + 31) / 32;
+    const uint32_t b0 = lane * per;
     uint32_t local = 0;
     for (uint32_t i = 0; i < per; ++i)
         if (b0 + i < nb)
             local += bins[b0 + i];
-    uint32_t total;
-    uint32_t run = block_excl_scan<kNT>(local, ws, &total);
+    uint32_t x = local;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1)
+    {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+        if (lane >= (uint32_t)d)
+            x += y;
+    }
+    uint32_t run = x - local;
     for (uint32_t i = 0; i < per; ++i)
         if (b0 + i < nb)
         {
@@ -149,7 +161,6 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
     uint32_t * bins = reinterpret_cast<uint32_t *>(sorted_d + kTile);
     uint32_t * excl = bins + nb;
     uint32_t * gbase = excl + nb;
-    uint32_t * ws = gbase + nb;
 
     for (uint32_t i = threadIdx.x; i < nb; i += kNT)
         bins[i] = 0;
@@ -174,7 +185,7 @@ __global__ void __launch_bounds__(kNT, 2) k_part_scatter(const __grid_constant__
         }
     }
     __syncthreads();
-    smem_bins_scan(bins, excl, nb, ws);
+    smem_bins_scan(bins, excl, nb);
     const uint64_t ebase = (uint64_t)tr.tile0 * nb;
     for (uint32_t d = threadIdx.x; d < nb; d += kNT)
         gbase[d] = offs[ebase + (uint64_t)d * tr.nt + tr.k];
