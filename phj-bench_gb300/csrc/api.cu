@@ -480,7 +480,21 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
             const bool split = bits[0] > 11;
             const Cols ptmp = split ? alloc_cols_like(s, P.schema, P.rows) : ppart;
             uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
-            radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            // a two-stage ring leaves shared memory on each SM for the build
+            // side's kernels running beside this pass (unless pinned)
+            const uint32_t pinned_stages = ctx->p1_stages;
+            if (!pinned_stages)
+                ctx->p1_stages = 2;
+            try
+            {
+                radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            }
+            catch (...)
+            {
+                ctx->p1_stages = pinned_stages;
+                throw;
+            }
+            ctx->p1_stages = pinned_stages;
             a.probe = ppart;
             PHJ_CUDA(cudaEventRecord(ev[6], ctx->stream));
         }
