@@ -295,6 +295,8 @@ def reference_arm(args, rank, world, dist):
     desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
     frac = args.cpu_probe_frac
+    if args.pass_bits:
+        bits = [int(x) for x in args.pass_bits.split(",")]
     if bits is None:
         bits = P.autotune_radix(bspec["rows"])
     if bspec["kind"] == 2:
@@ -344,6 +346,7 @@ def main():
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--scheme", default=None, choices=["phj-pure", "chj", "phj"])
     ap.add_argument("--bep-budget-mib", type=int, default=0, help="PHJ (BEP) whole-run probe budget (default: per-group budget x SMs)")
+    ap.add_argument("--pass-bits", default=None, help="radix bits per pass, e.g. 8,8 (overrides the workload's; no autotuning)")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-probe-frac", type=float, default=1 / 16)
     ap.add_argument("--no-cpu", action="store_true")
@@ -367,6 +370,8 @@ def main():
     import phj_gpu as P
     desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
     scheme = args.scheme or scheme
+    if args.pass_bits:
+        bits = [int(x) for x in args.pass_bits.split(",")]
     if args.scale != 1.0:
         scale_workload(args.workload, args.scale)
         desc, _, bspec, pspec, _ = WORKLOADS[args.workload]
