@@ -54,8 +54,8 @@ WORKLOADS = {
            dict(kind=2, rows=32 * M, seed=0xD1, key_seed=0x77, types=[0, 1, 4]),
            dict(kind=4, rows=128 * M, seed=0xD2, key_seed=0x77, types=[2], domain=None, match_permille=500), None),
     "c4": ("PHJ (BEP) under skew 64M x 512M: unique u64 build keys with a u64 payload; probe keys Zipf(1.0) ranks through a "
-           "seeded permutation onto the build keys, u32 payload; 3 passes x 6 bits; 32 MiB probe budget per CTA group "
-           "(one group per SM); lazy per-leaf build", "phj",
+           "seeded permutation onto the build keys, u32 payload; 3 passes x 6 bits (262,144 leaves, partitioned on the device "
+           "in 2 passes of 9 bits); 32 MiB probe budget per CTA group (one group per SM); lazy per-leaf build", "phj",
            dict(kind=0, rows=64 * M, seed=0xE1, key_seed=0x99, types=[3]),
            dict(kind=5, rows=512 * M, seed=0xE2, key_seed=0x99, types=[2], domain=64 * M, theta=1.0), [6, 6, 6]),
 }
