@@ -102,6 +102,54 @@ void * dalloc(phj_ctx * ctx, size_t bytes)
     return p;
 }
 
+namespace
+{
+struct SmallReadArgs
+{
+    const uint8_t * src[kMaxSmallReads];
+    uint32_t bytes[kMaxSmallReads];
+    uint32_t off[kMaxSmallReads];
+    uint32_t n;
+};
+
+__global__ void k_read_small(const __grid_constant__ SmallReadArgs r, uint8_t * dst)
+{
+    for (uint32_t i = 0; i < r.n; ++i)
+        for (uint32_t b = threadIdx.x; b < r.bytes[i]; b += blockDim.x)
+            dst[r.off[i] + b] = r.src[i][b];
+    __threadfence_system();
+}
+} // namespace
+
+void read_small(phj_ctx * ctx, std::initializer_list<SmallRead> reads)
+{
+    if (!ctx->host_small)
+    {
+        PHJ_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&ctx->host_small), kSmallReadBytes, cudaHostAllocMapped));
+        PHJ_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void **>(&ctx->host_small_dev), ctx->host_small, 0));
+    }
+    SmallReadArgs r{};
+    uint32_t off = 0;
+    for (const SmallRead & x : reads)
+    {
+        if (r.n == kMaxSmallReads || off + x.bytes > kSmallReadBytes)
+            throw Error(PHJ_ERR_CUDA, "internal: read_small over its buffer");
+        r.src[r.n] = static_cast<const uint8_t *>(x.src);
+        r.bytes[r.n] = x.bytes;
+        r.off[r.n++] = off;
+        off += (x.bytes + 7) & ~7u;
+    }
+    k_read_small<<<1, 32, 0, ctx->stream>>>(r, ctx->host_small_dev);
+    PHJ_LAUNCHED(ctx, "read_small");
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    off = 0;
+    for (const SmallRead & x : reads)
+    {
+        std::memcpy(x.dst, ctx->host_small + off, x.bytes);
+        off += (x.bytes + 7) & ~7u;
+    }
+}
+
 void dfree(phj_ctx * ctx, void * p)
 {
     if (!p)
@@ -396,8 +444,7 @@ phj_output * probe_into_output(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, 
 static void check_device_error(phj_ctx * ctx)
 {
     int e = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&e, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&e, ctx->d_err, sizeof(int)}});
     if (e != 0)
     {
         PHJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
@@ -930,6 +977,15 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
         res->e2e_wall_ms = event_ms(ev[0], ev[3]);
         res->peak_mem_bytes = ctx->peak_bytes;
     }
+    if (std::getenv("PHJ_DEBUG"))
+    {
+        // when each stage of each chunk finished, ms from the start
+        std::fprintf(stderr, "[phj] host join: build uploaded %.3f, built %.3f\n", event_ms(ev[0], build_up), event_ms(ev[0], ev[2]));
+        for (uint64_t c = 0; c < n_chunks; ++c)
+            std::fprintf(stderr, "[phj] chunk %llu (%llu rows): uploaded %.3f, input free %.3f, projected %.3f, downloaded %.3f\n",
+                         (unsigned long long)c, (unsigned long long)(start(c + 1) - start(c)), event_ms(ev[0], up[c]), event_ms(ev[0], used[c]),
+                         event_ms(ev[0], proj[c]), event_ms(ev[0], down[c]));
+    }
     if (total > out_cap)
         throw Error(PHJ_ERR_CAPACITY, "host output holds " + std::to_string(out_cap) + " rows; the join has " + std::to_string(total) +
                                           " (the first rows up to the capacity were written)");
@@ -1010,6 +1066,8 @@ void phj_ctx_destroy(phj_ctx * ctx)
         cudaFree(ctx->l2_flush);
     if (ctx->d_err)
         cudaFree(ctx->d_err);
+    if (ctx->host_small)
+        cudaFreeHost(ctx->host_small);
     for (cudaEvent_t e : ctx->event_pool)
         cudaEventDestroy(e);
     for (auto & lv : ctx->live)

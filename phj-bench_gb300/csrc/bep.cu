@@ -191,8 +191,7 @@ bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b)
         PHJ_LAUNCHED(ctx, "bep_build");
     }
     int dup = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&dup, b.any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&dup, b.any_dup, sizeof(int)}});
     return dup != 0;
 }
 } // namespace phjg

@@ -319,9 +319,7 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
     PHJ_LAUNCHED(ctx, "leaf_caps");
     scan_u32(ctx, s, caps, table_off, n_leaves);
     uint32_t host[2] = {0, 0};
-    PHJ_CUDA(cudaMemcpyAsync(&host[0], small, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(&host[1], table_off + n_leaves, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&host[0], small, sizeof(uint32_t)}, {&host[1], table_off + n_leaves, sizeof(uint32_t)}});
     lt.max_rows = host[0];
     // at least one aligned cell pair: the probe's first load reads two cells
     const uint64_t max_cap = lt.max_rows ? table_cells(lt.max_rows, ctx->table_cap_pct) : 2;
@@ -354,8 +352,7 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
                                                                                             smem_cells, lt.cells, lt.next, lt.meta, any_dup);
         PHJ_LAUNCHED(ctx, "build_leaf");
     }
-    PHJ_CUDA(cudaMemcpyAsync(&lt.any_dup, any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&lt.any_dup, any_dup, sizeof(int)}});
 }
 
 void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uint32_t slot_bits, LeafTables & lt)
@@ -384,8 +381,7 @@ void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uin
     PHJ_LAUNCHED(ctx, "chj_caps");
     scan_u32(ctx, s, caps, table_off, n_slots);
     uint32_t total = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&total, table_off + n_slots, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&total, table_off + n_slots, sizeof(uint32_t)}});
     lt.total_cells = total;
     lt.meta = s.get<LeafMeta>(n_slots);
     lt.cells = s.get<Cell>(total);
@@ -403,8 +399,7 @@ void build_global_table(phj_ctx * ctx, Scratch & s, const phj_table & build, uin
                                                    lt.meta, lt.next, any_dup);
         PHJ_LAUNCHED(ctx, "chj_insert");
     }
-    PHJ_CUDA(cudaMemcpyAsync(&lt.any_dup, any_dup, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&lt.any_dup, any_dup, sizeof(int)}});
 }
 
 } // namespace phjg

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <initializer_list>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -95,6 +96,8 @@ struct phj_ctx
     void * l2_flush = nullptr;
     size_t l2_flush_bytes = 0;
     int * d_err = nullptr; // device error word: bounded waits that gave up
+    uint8_t * host_small = nullptr;     // mapped pinned buffer of read_small
+    uint8_t * host_small_dev = nullptr; // its device address
     // Options (phj_ctx_set_int).
     int probe_materialize = -1; // -1 auto, 0 never, 1 always
     int64_t wait_limit_ms = 1000; // bound of a device wait on another warp's work
@@ -134,6 +137,22 @@ namespace phjg
 // ----- allocation (stream-ordered pool of the context) ---------------------
 void * dalloc(phj_ctx * ctx, size_t bytes);
 void dfree(phj_ctx * ctx, void * p);
+
+// Small device-to-host reads (row counts, flags, the error word).  A kernel
+// stores the values into the context's mapped pinned buffer and the host
+// waits for the context's stream.  A copy-engine read would queue behind a
+// large download in flight on another stream (the host-buffer join
+// downloads one chunk's output while it probes the next); the kernel does
+// not.  At most kMaxSmallReads values of at most kSmallReadBytes in all.
+struct SmallRead
+{
+    void * dst;
+    const void * src;
+    uint32_t bytes;
+};
+constexpr uint32_t kMaxSmallReads = 8;
+constexpr uint32_t kSmallReadBytes = 256;
+void read_small(phj_ctx * ctx, std::initializer_list<SmallRead> reads);
 void reset_accounting(phj_ctx * ctx);
 
 template <class T>

@@ -652,8 +652,7 @@ uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, uint32
     launch_any(ctx, a, nullptr, heads, counts, 0, true, "probe_lookup", a.probe_rows * (8 + 4));
     scan_u32(ctx, s, counts, counts, n_chunks);
     unsigned long long total = 0;
-    PHJ_CUDA(cudaMemcpyAsync(&total, a.out_rows64, sizeof(total), cudaMemcpyDeviceToHost, ctx->stream));
-    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    read_small(ctx, {{&total, a.out_rows64, sizeof(total)}});
     if (total >= (1ull << 32))
         throw Error(PHJ_ERR_CAPACITY, "the join has " + std::to_string(total) + " output rows; the device schemes place at most 2^32 - 1");
     return total;
