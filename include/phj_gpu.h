@@ -162,6 +162,10 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *   "p1_tile_rows", "p1_stages": tile rows (1024/2048/4096) and bulk-copy
  *        ring depth (2..4) of the first radix pass, 0 (default) chosen per
  *        row width;
+ *   "pack_build": 1 (default) packs the build payloads row-major (16 bytes a
+ *        row) for CHJ and PHJ-PURE joins without repeated build keys whose
+ *        2+ build payload columns fit 16 bytes, so the projection gathers one
+ *        value per output row; 0 gathers column by column;
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
  *        leaf BUILDING before the probe, so its waits run out. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);

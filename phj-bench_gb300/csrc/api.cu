@@ -480,6 +480,7 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     a.uniform_block_rows = B.uniform_block_rows;
     a.any_dup = lt.any_dup;
     a.uniform_log2cap = -1;
+    pack_build_payloads(ctx, s, a, B.rows);
     phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(e2));
@@ -572,6 +573,10 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
         // repeated keys: each key's rows made contiguous, so the probe
         // expands a match as a row range
         grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
+        // build payloads packed for the projection (no repeated key)
+        a.build = payload_cols(grouped ? btmp : bpart);
+        a.any_dup = lt.any_dup;
+        pack_build_payloads(ctx, s, a, B.rows);
         PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
     }
     catch (...)
@@ -873,6 +878,8 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     a.chj = 0;
     a.any_dup = lt.any_dup;
     a.uniform_log2cap = lt.uniform_log2cap;
+    // (build payloads stay in columns: the host link bounds this path, and
+    // packing them would only add to the time before the first download)
     const bool mat = materialize_probe(ctx, lt, *B, n_leaves) && P_rows > 0;
     const Cols ppart = mat ? alloc_cols_like(s, hp.schema, C) : Cols{};
     const Cols ptmp = mat && bits[0] > 11 ? alloc_cols_like(s, hp.schema, C) : ppart;
@@ -1115,6 +1122,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->p1_tile_rows = (uint32_t)value;
     else if (std::strcmp(name, "p1_stages") == 0 && (value == 0 || (value >= 2 && value <= 4)))
         ctx->p1_stages = (uint32_t)value;
+    else if (std::strcmp(name, "pack_build") == 0 && (value == 0 || value == 1))
+        ctx->pack_build = (int)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
     else
@@ -1140,6 +1149,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->p1_tile_rows;
     else if (std::strcmp(name, "p1_stages") == 0)
         *value = ctx->p1_stages;
+    else if (std::strcmp(name, "pack_build") == 0)
+        *value = ctx->pack_build;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
     else if (std::strcmp(name, "device") == 0)

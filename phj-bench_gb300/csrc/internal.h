@@ -105,6 +105,7 @@ struct phj_ctx
     uint32_t table_cap_pct = 200; // leaf table cells >= rows * pct / 100 (power of two)
     uint32_t p1_tile_rows = 0;    // first radix pass: rows per staged tile (0: chosen per row width)
     uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
+    int pack_build = 1;           // pack unique-key build payloads row-major for the projection (0: columns)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
     LeafMark leaf_mark;           // consumed by the next first radix pass
 };
@@ -275,6 +276,13 @@ struct ProbeArgs
     uint32_t * row_cnt;  // per probe row: its match count (when keys repeat)
     uint32_t * flat;     // chained duplicates: build row of every output row
     unsigned long long * out_rows64; // the lookup's 64-bit count of output rows
+    // Build payloads also packed row-major (no repeated key; two or more
+    // columns of 1-8 bytes, 16 bytes in all): build row r's payloads in the
+    // 16 bytes at packed[r], column c at byte packed_off[c].  The projection
+    // then gathers one 16-byte value per output row instead of one per
+    // column.  nullptr: columns only.
+    const uint4 * packed;
+    uint8_t packed_off[kMaxCols];
 };
 // PHJ/BEP lazy leaf tables.  Per probe batch: the leaves the batch touches
 // are flagged (one eviction per leaf and batch), the touched leaves still
@@ -309,6 +317,9 @@ void set_bep_smem_limits(int smem_optin);
 
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);
+// Sets a.packed (and packed_off) when the plain projection can use packed
+// build payloads (a.any_dup known, build_rows rows in a.build).
+void pack_build_payloads(phj_ctx * ctx, Scratch & s, ProbeArgs & a, uint64_t build_rows);
 // The two halves: lookups + chunk-offset scan (returns the output rows), and
 // the projection into `out` from row `out_base` on.
 uint64_t probe_chunks(uint64_t probe_rows);

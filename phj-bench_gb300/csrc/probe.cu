@@ -418,6 +418,123 @@ __global__ void __launch_bounds__(kPNT, kWide ? 1 : 4) k_probe_project(const __g
     }
 }
 
+// Build payload columns of the packed projection: output column, width and
+// byte offset in the packed 16-byte row.
+struct PackedCols
+{
+    void * dst[kMaxCols];
+    uint8_t width[kMaxCols];
+    uint8_t off[kMaxCols];
+    uint32_t n;
+};
+
+// One build payload column of a half from the gathered packed rows.  The
+// offset is a multiple of the width, so a value lies in one 8-byte half.
+template <class T>
+__device__ __forceinline__ void packed_column(const uint4 (&row)[kPH], uint32_t off, void * dst_v, uint64_t base, const uint32_t (&rel)[kPH],
+                                              uint32_t one)
+{
+    T * dst = static_cast<T *>(dst_v) + base;
+#pragma unroll
+    for (int u = 0; u < kPH; ++u)
+        if (one >> u & 1u)
+        {
+            if constexpr (sizeof(T) == 8)
+                __stcs(dst + rel[u], off ? ((uint64_t)row[u].w << 32 | row[u].z) : ((uint64_t)row[u].y << 32 | row[u].x));
+            else
+            {
+                // the 32-bit word holding the value, then its bytes
+                const uint32_t wd = (off & 8u) ? ((off & 4u) ? row[u].w : row[u].z) : ((off & 4u) ? row[u].y : row[u].x);
+                __stcs(dst + rel[u], (T)(wd >> ((off & 3u) * 8u)));
+            }
+        }
+}
+
+// Projection when no key repeats and the build payloads are packed: as
+// k_probe_project, with one 16-byte gather per output row for all build
+// payload columns (fewer random requests through L1, the kernel's busiest
+// path); pc holds the key column and the probe payload columns only.
+template <bool kWide>
+__global__ void __launch_bounds__(kPNT, kWide ? 1 : 4) k_probe_project_packed(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+                                                                           const __grid_constant__ PackedCols bc, const uint32_t * __restrict__ heads,
+                                                                           const uint32_t * __restrict__ offs, uint64_t out_cap)
+{
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+    const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
+    for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
+    {
+        uint64_t base = offs[chunk];
+#pragma unroll 1
+        for (int half = 0; half < kPRPT / kPH; ++half)
+        {
+            const uint64_t row0 = chunk * kWChunk + (uint64_t)half * kPH * 32 + lane;
+            uint32_t brow[kPH], prow[kPH], one = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                const uint64_t row = row0 + (uint64_t)k * 32;
+                prow[k] = (uint32_t)row;
+                brow[k] = row < a.probe_rows ? __ldcs(heads + row) : kNoMatch;
+                if (brow[k] != kNoMatch)
+                    one |= 1u << k;
+            }
+            uint32_t rel[kPH], running = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                const uint32_t m = __ballot_sync(0xffffffffu, one >> k & 1u);
+                rel[k] = running + __popc(m & ((1u << lane) - 1u));
+                running += __popc(m);
+                if (base + rel[k] >= out_cap)
+                    one &= ~(1u << k);
+            }
+            // key and probe payload columns first (prow is then dead)
+            project_all<kWide>(pc, brow, prow, base, rel, one);
+            {
+                uint4 row[kPH];
+#pragma unroll
+                for (int u = 0; u < kPH; ++u)
+                    if (one >> u & 1u)
+                        row[u] = __ldg(a.packed + brow[u]);
+#pragma unroll 1
+                for (uint32_t c = 0; c < bc.n; ++c)
+                    switch (bc.width[c])
+                    {
+                        case 1: packed_column<uint8_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        case 2: packed_column<uint16_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        case 4: packed_column<uint32_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        default: packed_column<uint64_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                    }
+            }
+            base += running;
+        }
+    }
+}
+
+// Packs build payload columns row-major: row r's column c at byte off[c] of
+// the 16 bytes at out[r] (unused bytes zero).
+__global__ void k_pack_rows(const __grid_constant__ Cols in, uint64_t n, const __grid_constant__ PackedCols pk, uint4 * __restrict__ out)
+{
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x)
+    {
+        uint64_t h[2] = {0, 0};
+        for (uint32_t c = 0; c < in.n; ++c)
+        {
+            uint64_t v;
+            switch (in.width[c])
+            {
+                case 1: v = static_cast<const uint8_t *>(in.col[c])[r]; break;
+                case 2: v = static_cast<const uint16_t *>(in.col[c])[r]; break;
+                case 4: v = static_cast<const uint32_t *>(in.col[c])[r]; break;
+                default: v = static_cast<const uint64_t *>(in.col[c])[r]; break;
+            }
+            h[pk.off[c] >> 3] |= v << ((pk.off[c] & 7u) * 8u);
+        }
+        out[r] = make_uint4((uint32_t)h[0], (uint32_t)(h[0] >> 32), (uint32_t)h[1], (uint32_t)(h[1] >> 32));
+    }
+}
+
 // Chained duplicates (CHJ, leaves too large to group, lazily built BEP
 // tables): each probe row's chain is walked once and its build rows are
 // written to a flat array at the row's output offsets, which the range
@@ -577,9 +694,17 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
         wide = wide || a.build.width[c] > 8;
     for (uint32_t c = 0; c < a.probe.n; ++c)
         wide = wide || a.probe.width[c] > 8;
+    // packed build payloads: one gather per output row for all of them
+    const bool packed = !lookup && proj == 0 && a.packed;
+    bool wide_probe = false;
+    for (uint32_t c = 0; c < a.probe.n; ++c)
+        wide_probe = wide_probe || a.probe.width[c] > 8;
     int per_sm = 0;
     if (lookup)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, lk, kPNT, 0));
+    else if (packed)
+        PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide_probe ? k_probe_project_packed<true> : k_probe_project_packed<false>,
+                                                               kPNT, 0));
     else if (proj == 0)
         PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, wide ? k_probe_project<kMode, true> : k_probe_project<kMode, false>, kPNT, 0));
     else
@@ -602,6 +727,32 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
     KTimer kt(ctx, name, a.probe_rows, bytes);
     if (lookup)
         lk<<<grid, kPNT, 0, ctx->stream>>>(a, heads, counts);
+    else if (packed)
+    {
+        // key column and probe payloads by column, build payloads packed
+        ProjCols pc{};
+        PackedCols bc{};
+        const ProjCols all = proj_cols(a, *o);
+        for (uint32_t j = 0; j < all.n; ++j)
+            if (!all.by_build[j])
+            {
+                pc.src[pc.n] = all.src[j];
+                pc.dst[pc.n] = all.dst[j];
+                pc.width[pc.n] = all.width[j];
+                pc.by_build[pc.n++] = 0;
+            }
+        for (uint32_t c = 0; c < a.build.n; ++c)
+        {
+            bc.dst[c] = o->left[c];
+            bc.width[c] = (uint8_t)a.build.width[c];
+            bc.off[c] = a.packed_off[c];
+        }
+        bc.n = a.build.n;
+        if (wide_probe)
+            k_probe_project_packed<true><<<grid, kPNT, 0, ctx->stream>>>(a, pc, bc, heads, counts, cap);
+        else
+            k_probe_project_packed<false><<<grid, kPNT, 0, ctx->stream>>>(a, pc, bc, heads, counts, cap);
+    }
     else if (proj == 0 && wide)
         k_probe_project<kMode, true><<<grid, kPNT, 0, ctx->stream>>>(a, proj_cols(a, *o), heads, counts, cap);
     else if (proj == 0)
@@ -656,6 +807,41 @@ uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, uint32
     if (total >= (1ull << 32))
         throw Error(PHJ_ERR_CAPACITY, "the join has " + std::to_string(total) + " output rows; the device schemes place at most 2^32 - 1");
     return total;
+}
+
+void pack_build_payloads(phj_ctx * ctx, Scratch & s, ProbeArgs & a, uint64_t build_rows)
+{
+    a.packed = nullptr;
+    if (!ctx->pack_build || a.any_dup || a.build.n < 2 || build_rows == 0)
+        return;
+    // widest column first, so every offset is a multiple of its width
+    uint32_t order[kMaxCols];
+    for (uint32_t c = 0; c < a.build.n; ++c)
+        order[c] = c;
+    std::stable_sort(order, order + a.build.n, [&](uint32_t x, uint32_t y) { return a.build.width[x] > a.build.width[y]; });
+    uint32_t off = 0;
+    PackedCols pk{};
+    for (uint32_t i = 0; i < a.build.n; ++i)
+    {
+        const uint32_t c = order[i];
+        if (a.build.width[c] > 8)
+            return;
+        pk.off[c] = (uint8_t)off;
+        off += a.build.width[c];
+    }
+    if (off > 16)
+        return;
+    pk.n = a.build.n;
+    uint4 * p = s.get<uint4>(build_rows);
+    {
+        KTimer kt(ctx, "pack_build", build_rows, build_rows * (off + 16));
+        k_pack_rows<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(build_rows, 256), (uint64_t)ctx->num_sms * 8)), 256, 0, ctx->stream>>>(
+            a.build, build_rows, pk, p);
+        PHJ_LAUNCHED(ctx, "pack_build");
+    }
+    for (uint32_t c = 0; c < a.build.n; ++c)
+        a.packed_off[c] = pk.off[c];
+    a.packed = p;
 }
 
 uint64_t probe_chunks(uint64_t probe_rows)

@@ -292,3 +292,37 @@ def test_host_buffer_short_capacity(ctx):
     keys, left, right = host_out(ctx, b, p, len(expected))
     rows, _ = ctx.run_phj_pure_host(b, p, [4, 4], keys, left, right)
     assert rows == len(expected)
+
+
+@pytest.mark.parametrize("pack", [1, 0])
+@pytest.mark.parametrize("build_types", [[P.U64, P.U32], [P.U8, P.U16, P.U32], [P.U32, P.U64, P.U32], [P.U64, P.U64],
+                                         [P.U64, P.U64, P.U8], [P.U16]])
+def test_packed_build_payloads(ctx, pack, build_types):
+    # With unique build keys and 2+ build payload columns of at most 16 bytes
+    # in all, the build payloads are packed row-major and the projection
+    # gathers one 16-byte value per output row (pack 1); otherwise (and with
+    # pack 0) it gathers each column.  Offsets follow the widest-first
+    # packing; 17 bytes or one column stay unpacked.
+    bk = G.gen_keys(0, 7000, 31, 9)
+    b = P.BlockStream(build_types, bk, G.payload_columns(32, build_types, 7000))
+    rows = 256 * 50 + 19
+    p = P.BlockStream([P.U32], G.gen_keys(4, rows, 33, 9, domain=7000, match_permille=800), G.payload_columns(34, [P.U32], rows))
+    ctx.set_int("pack_build", pack)
+    try:
+        for scheme, bits in (("phj-pure", [4, 3]), ("chj", None)):
+            for materialize in (0, 1):
+                jo, fp, _ = run(ctx, scheme, b, p, bits, materialize)
+                check(b, p, jo, fp)
+        # host-buffer PHJ-PURE, probe side in 4096-row chunks
+        expected = O.join_rows(b, p)
+        ctx.set_int("host_chunk_rows", 4096)
+        try:
+            keys, left, right = host_out(ctx, b, p, len(expected))
+            n, _ = ctx.run_phj_pure_host(b, p, [4, 3], keys, left, right)
+        finally:
+            ctx.set_int("host_chunk_rows", 16 << 20)
+        assert n == len(expected)
+        jo = P.JoinOutput(b.types, p.types, keys[:n], [c[:n] for c in left], [c[:n] for c in right])
+        assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
+    finally:
+        ctx.set_int("pack_build", 1)
