@@ -454,6 +454,24 @@ static void check_device_error(phj_ctx * ctx)
     }
 }
 
+// With PHJ_DEBUG set: each timed kernel of the run with its start and end,
+// ms from `t0` (kernels on both streams of a scheme).
+static void debug_timeline(phj_ctx * ctx, cudaEvent_t t0)
+{
+    if (!std::getenv("PHJ_DEBUG") || !ctx->time_kernels)
+        return;
+    for (const auto & r : ctx->records)
+    {
+        float a = 0.f, b = 0.f;
+        if (cudaEventElapsedTime(&a, t0, r.start) != cudaSuccess || cudaEventElapsedTime(&b, t0, r.stop) != cudaSuccess)
+        {
+            cudaGetLastError();
+            continue;
+        }
+        std::fprintf(stderr, "[phj] timeline %-22s %8.3f %8.3f %7.3f\n", r.name.c_str(), a, b, b - a);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // schemes
 // ---------------------------------------------------------------------------
@@ -604,6 +622,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     PHJ_CUDA(cudaEventRecord(ev[4], ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(ev[4]));
     check_device_error(ctx);
+    debug_timeline(ctx, ev[0]);
     if (res)
     {
         fill_phase(res->build_shuffle, event_ms(ev[0], ev[1]), B.rows);

@@ -330,8 +330,12 @@ __device__ __forceinline__ void p1_write_column(const uint8_t * buf, T * __restr
             dst[dest[j]] = b[src[j]];
 }
 
+// At most 64 registers a thread (launch bound of two CTAs, though shared
+// memory admits one): the other half of the register file stays free, so
+// the build side's later pass (scan, histogram, scatter) runs beside the
+// probe side's first pass instead of waiting for it to retire.
 template <int RPT>
-__global__ void __launch_bounds__(kP1NT, 1) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
+__global__ void __launch_bounds__(kP1NT, 2) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
                                                          const __grid_constant__ P1Smem sm, uint32_t stages, const uint32_t * __restrict__ offs,
                                                          int use_tma, int * __restrict__ err)
 {
