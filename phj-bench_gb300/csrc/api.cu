@@ -533,6 +533,13 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     a.probe = cols_of(P);
     const bool mat = materialize_probe_estimate(ctx, B) && P.rows > 0;
     cudaStream_t main_stream = ctx->stream;
+    // the two sides' partition passes share the GPU: register-capped scatter
+    struct BesideGuard
+    {
+        phj_ctx * c;
+        ~BesideGuard() { c->p1_beside = false; }
+    } beside_guard{ctx};
+    ctx->p1_beside = mat;
     if (mat)
     {
         if (!ctx->side)

@@ -330,12 +330,13 @@ __device__ __forceinline__ void p1_write_column(const uint8_t * buf, T * __restr
             dst[dest[j]] = b[src[j]];
 }
 
-// At most 64 registers a thread (launch bound of two CTAs, though shared
-// memory admits one): the other half of the register file stays free, so
-// the build side's later pass (scan, histogram, scatter) runs beside the
-// probe side's first pass instead of waiting for it to retire.
-template <int RPT>
-__global__ void __launch_bounds__(kP1NT, 2) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
+// kMinB 2 holds the kernel to 64 registers a thread (a launch bound of two
+// CTAs, though shared memory admits one): half of the register file stays
+// free, so the build side's later pass (scan, histogram, scatter) runs
+// beside the probe side's first pass instead of waiting for it to retire.
+// A pass that runs alone takes kMinB 1 (72 registers).
+template <int RPT, int kMinB>
+__global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_constant__ Cols in, const __grid_constant__ Cols out, P1Geom g,
                                                          const __grid_constant__ P1Smem sm, uint32_t stages, const uint32_t * __restrict__ offs,
                                                          int use_tma, int * __restrict__ err)
 {
@@ -618,7 +619,8 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
     sm.buf_bytes = (off + 127) & ~127u;
     const size_t need = (size_t)stages * sm.buf_bytes + 4ull * kT + 3ull * nb * 4;
     int per_sm = 1;
-    auto kern = rpt == 8 ? k_p1_scatter<8> : rpt == 4 ? k_p1_scatter<4> : k_p1_scatter<2>;
+    auto kern = ctx->p1_beside ? (rpt == 8 ? k_p1_scatter<8, 2> : rpt == 4 ? k_p1_scatter<4, 2> : k_p1_scatter<2, 2>)
+                               : (rpt == 8 ? k_p1_scatter<8, 1> : rpt == 4 ? k_p1_scatter<4, 1> : k_p1_scatter<2, 1>);
     PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kP1NT, need));
     const uint64_t n_tiles = ceil_div(n, kT);
     const uint32_t G = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->num_sms * std::max(per_sm, 1)));
@@ -739,11 +741,14 @@ void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, co
 
 void set_partition_smem_limits(int smem_optin)
 {
-    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
-    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<8, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<4, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<2, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<8, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<4, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
+    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<2, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
     PHJ_CUDA(cudaFuncSetAttribute(k_p1_hist, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   (int)std::min<size_t>(((1u << kMaxPassBits) + (1u << 20) / 32) * sizeof(uint32_t), (size_t)smem_optin - 1024)));
-    PHJ_CUDA(cudaFuncSetAttribute(k_p1_scatter<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_optin - 1024));
     // The scatter kernel stages a 4096-row tile of the widest column (<= 16
     // bytes) plus digit bins: up to ~96 KiB.
     const size_t need = (size_t)kTile * 16 + (size_t)kTile * sizeof(uint16_t) + 3ull * (1u << kMaxPassBits) * sizeof(uint32_t) + 128;
