@@ -503,6 +503,7 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(e2));
     check_device_error(ctx);
+    debug_timeline(ctx, e0);
     if (res)
     {
         fill_phase(res->build, event_ms(e0, e1), B.rows);
@@ -666,13 +667,80 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
         e = take_event(ctx);
     PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
 
-    // -------- BUILD SHUFFLE, full leaf depth (src/PHJBep.cpp:128-141) --------
+    // probe batches: buffers, and the touched-leaf bitmap their first passes fill
+    const uint64_t row_bytes = 8 + schema_bytes(P.schema);
+    const uint64_t budget_rows = (budget_mib << 20) / row_bytes;
+    const uint64_t batch_rows = std::min<uint64_t>(std::max<uint64_t>(P.rows, 1), std::max<uint64_t>(4096, budget_rows & ~uint64_t(255)));
+    const uint32_t p1 = 1u << bits[0];
+    const Cols pin = cols_of(P);
+    const Cols ppart = alloc_cols_like(s, P.schema, batch_rows);
+    const Cols ptmp = bits[0] > 11 ? alloc_cols_like(s, P.schema, batch_rows) : ppart;
+    uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
+    uint32_t * touched = s.get<uint32_t>((n_leaves + 31) / 32);
+    PHJ_CUDA(cudaMemsetAsync(touched, 0, (size_t)((n_leaves + 31) / 32) * 4, ctx->stream));
     const Cols bin = cols_of(B);
     const Cols bpart = alloc_cols_like(s, B.schema, B.rows);
     const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
     uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
-    radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+
+    // -------- PROBE SHUFFLE of the first batch, on the side stream beside
+    // the build shuffle (it needs nothing of the build side) --------
+    cudaStream_t main_stream = ctx->stream;
+    const bool early = P.rows > 0;
+    cudaEvent_t es[2] = {take_event(ctx), take_event(ctx)}; // the side pass's span
+    struct BesideGuard
+    {
+        phj_ctx * c;
+        ~BesideGuard() { c->p1_beside = false; }
+    } beside_guard{ctx};
+    ctx->p1_beside = early;
+    if (early)
+    {
+        if (!ctx->side)
+            PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking));
+        cudaEvent_t ready = take_event(ctx);
+        PHJ_CUDA(cudaEventRecord(ready, ctx->stream));
+        PHJ_CUDA(cudaStreamWaitEvent(ctx->side, ready, 0));
+        ctx->stream = ctx->side;
+        const uint32_t pinned_stages = ctx->p1_stages;
+        try
+        {
+            PHJ_CUDA(cudaEventRecord(es[0], ctx->stream));
+            // the batch's first radix pass also flags the leaves its rows
+            // touch (its histogram reads every key once anyway); a two-stage
+            // ring leaves shared memory for the build side's kernels
+            ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
+            if (!pinned_stages)
+                ctx->p1_stages = 2;
+            radix_partition(ctx, s, pin, std::min(batch_rows, P.rows), {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            ctx->p1_stages = pinned_stages;
+            ctx->leaf_mark = LeafMark{};
+            PHJ_CUDA(cudaEventRecord(es[1], ctx->stream));
+        }
+        catch (...)
+        {
+            ctx->p1_stages = pinned_stages;
+            ctx->leaf_mark = LeafMark{};
+            ctx->stream = main_stream;
+            cudaStreamSynchronize(ctx->side);
+            throw;
+        }
+        ctx->stream = main_stream;
+    }
+
+    // -------- BUILD SHUFFLE, full leaf depth (src/PHJBep.cpp:128-141) --------
+    try
+    {
+        radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    }
+    catch (...)
+    {
+        if (early)
+            cudaStreamSynchronize(ctx->side); // its buffers are freed with the scratch
+        throw;
+    }
     PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+    ctx->p1_beside = false;
 
     // -------- BUILD: table layout only; cells are built on first use --------
     LeafTables lt;
@@ -687,9 +755,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
 
     unsigned long long * ctr = s.get<unsigned long long>(4);
-    uint32_t * touched = s.get<uint32_t>((n_leaves + 31) / 32);
     PHJ_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(touched, 0, (size_t)((n_leaves + 31) / 32) * 4, ctx->stream));
 
     ProbeArgs a{};
     a.build = payload_cols(bpart);
@@ -720,14 +786,6 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     PHJ_CUDA(cudaMemsetAsync(bl.any_dup, 0, sizeof(int), ctx->stream));
 
     // -------- PROBE: budget-sized batches --------
-    const uint64_t row_bytes = 8 + schema_bytes(P.schema);
-    const uint64_t budget_rows = (budget_mib << 20) / row_bytes;
-    const uint64_t batch_rows = std::min<uint64_t>(std::max<uint64_t>(P.rows, 1), std::max<uint64_t>(4096, budget_rows & ~uint64_t(255)));
-    const uint32_t p1 = 1u << bits[0];
-    const Cols pin = cols_of(P);
-    const Cols ppart = alloc_cols_like(s, P.schema, batch_rows);
-    const Cols ptmp = bits[0] > 11 ? alloc_cols_like(s, P.schema, batch_rows) : ppart;
-    uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
     uint32_t * heads = s.get<uint32_t>(batch_rows);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(batch_rows) + 1);
     a.row_cnt = s.get<uint32_t>(batch_rows); // match counts when keys repeat
@@ -743,11 +801,16 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             peak_rows = std::max(peak_rows, n_b);
             Scratch sb(ctx);
             PHJ_CUDA(cudaEventRecord(eb[0], ctx->stream));
-            // the batch's first radix pass also flags the leaves its rows
-            // touch (its histogram reads every key once anyway)
-            ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
-            radix_partition(ctx, sb, cols_from(pin, r0), n_b, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
-            ctx->leaf_mark = LeafMark{};
+            if (r0 == 0)
+                PHJ_CUDA(cudaStreamWaitEvent(ctx->stream, es[1], 0)); // the first batch's pass ran on the side stream
+            else
+            {
+                // the batch's first radix pass also flags the leaves its
+                // rows touch (its histogram reads every key once anyway)
+                ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
+                radix_partition(ctx, sb, cols_from(pin, r0), n_b, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+                ctx->leaf_mark = LeafMark{};
+            }
             k_count_nonempty<<<(unsigned)ceil_div(p1, 256), 256, 0, ctx->stream>>>(poff, p1, ctr + 3);
             PHJ_LAUNCHED(ctx, "count_refinements");
             PHJ_CUDA(cudaEventRecord(eb[1], ctx->stream));
@@ -771,7 +834,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             total += rows;
             PHJ_CUDA(cudaEventRecord(eb[2], ctx->stream));
             PHJ_CUDA(cudaEventSynchronize(eb[2]));
-            t_shuffle += event_ms(eb[0], eb[1]);
+            t_shuffle += r0 == 0 ? event_ms(es[0], es[1]) : event_ms(eb[0], eb[1]);
             t_lazy += event_ms(eb[3], eb[4]);
             t_probe += event_ms(eb[4], eb[2]);
         }
@@ -781,6 +844,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
         PHJ_CUDA(cudaEventRecord(eb[0], ctx->stream));
         PHJ_CUDA(cudaEventSynchronize(eb[0]));
         check_device_error(ctx);
+        debug_timeline(ctx, ev[0]);
     }
     catch (...)
     {
