@@ -593,16 +593,20 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
         radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
         PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
 
+        // build payloads packed for the projection, ahead of the tables
+        // (beside the probe side's first pass); dropped if a key repeats
+        a.build = payload_cols(bpart);
+        a.any_dup = 0;
+        pack_build_payloads(ctx, s, a, B.rows);
+
         // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
         lt.next = s.get<uint64_t>(B.rows);
         build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt);
         // repeated keys: each key's rows made contiguous, so the probe
         // expands a match as a row range
         grouped = group_leaf_duplicates(ctx, bpart, btmp, leaf_off, n_leaves, lt);
-        // build payloads packed for the projection (no repeated key)
-        a.build = payload_cols(grouped ? btmp : bpart);
-        a.any_dup = lt.any_dup;
-        pack_build_payloads(ctx, s, a, B.rows);
+        if (lt.any_dup)
+            a.packed = nullptr;
         PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
     }
     catch (...)
