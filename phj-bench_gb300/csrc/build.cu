@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(kBuildNT) k_group_leaf(const __grid_constant__
                                                          const uint32_t * __restrict__ leaf_off, const LeafMeta * __restrict__ meta,
                                                          Cell * __restrict__ cells, uint64_t * __restrict__ next)
 {
-    extern __shared__ uint32_t gsh[]; // cnt[cap] | start[cap] | fill[cap]
+    extern __shared__ uint32_t gsh[]; // cnt[cap] | start[cap] | fill[cap] | cell of each row[cap]
     __shared__ uint32_t warp_sums[kBuildNT / 32];
     const uint32_t l = blockIdx.x;
     const uint32_t r0 = leaf_off[l], r = leaf_off[l + 1] - r0;
@@ -156,37 +156,42 @@ __global__ void __launch_bounds__(kBuildNT) k_group_leaf(const __grid_constant__
     uint32_t * cnt = gsh;
     uint32_t * start = gsh + cap;
     uint32_t * fill = gsh + 2 * cap;
+    uint32_t * rowcell = gsh + 3 * cap; // a leaf has at most cap rows
     for (uint32_t i = threadIdx.x; i < cap; i += kBuildNT)
         cnt[i] = 0;
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
-    {
-        const uint64_t k = src.keys[r0 + i];
-        atomicAdd(&cnt[cell_of(tab, cap, int_hash64(k), k)], 1u);
-    }
-    __syncthreads();
-    uint32_t running = 0;
-    for (uint32_t b = 0; b < cap; b += kBuildNT)
-    {
-        const uint32_t v = b + threadIdx.x < cap ? cnt[b + threadIdx.x] : 0u;
-        uint32_t tot;
-        const uint32_t ex = block_excl_scan<kBuildNT>(v, warp_sums, &tot);
-        if (b + threadIdx.x < cap)
-        {
-            start[b + threadIdx.x] = running + ex;
-            fill[b + threadIdx.x] = running + ex;
-        }
-        running += tot;
-        __syncthreads();
-    }
-    for (uint32_t c = threadIdx.x; c < cap; c += kBuildNT)
-        if (cnt[c])
-            tab[c].ref = make_ref(cnt[c], r0 + start[c]);
-    __syncthreads();
+    // each row's cell, found once and kept for the placement below
     for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
     {
         const uint64_t k = src.keys[r0 + i];
         const uint32_t c = cell_of(tab, cap, int_hash64(k), k);
+        rowcell[i] = c;
+        atomicAdd(&cnt[c], 1u);
+    }
+    __syncthreads();
+    // one block scan: thread t owns cells [t * per, (t + 1) * per)
+    const uint32_t per = (cap + kBuildNT - 1) / kBuildNT;
+    const uint32_t c0 = threadIdx.x * per;
+    uint32_t local = 0;
+    for (uint32_t j = 0; j < per; ++j)
+        if (c0 + j < cap)
+            local += cnt[c0 + j];
+    uint32_t tot;
+    uint32_t run = block_excl_scan<kBuildNT>(local, warp_sums, &tot);
+    for (uint32_t j = 0; j < per; ++j)
+        if (c0 + j < cap)
+        {
+            const uint32_t c = c0 + j, v = cnt[c];
+            start[c] = run;
+            fill[c] = run;
+            if (v)
+                tab[c].ref = make_ref(v, r0 + run);
+            run += v;
+        }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < r; i += kBuildNT)
+    {
+        const uint32_t c = rowcell[i];
         const uint32_t slot = atomicAdd(&fill[c], 1u);
         const uint64_t pos = (uint64_t)r0 + slot;
         copy_row(src, r0 + i, dst, pos);
@@ -275,7 +280,7 @@ void set_build_smem_limits(int smem_optin)
     PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf<kBuildNT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
     PHJ_CUDA(cudaFuncSetAttribute(k_build_leaf<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(need, (size_t)smem_optin - 1024)));
     PHJ_CUDA(cudaFuncSetAttribute(k_group_leaf, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)std::min<size_t>((size_t)kSmemCellsMax * 12, (size_t)smem_optin - 1024)));
+                                  (int)std::min<size_t>((size_t)kSmemCellsMax * 16, (size_t)smem_optin - 1024)));
 }
 
 bool group_leaf_duplicates(phj_ctx * ctx, const Cols & src, const Cols & dst, const uint32_t * leaf_off, uint32_t n_leaves, const LeafTables & lt)
@@ -287,7 +292,7 @@ bool group_leaf_duplicates(phj_ctx * ctx, const Cols & src, const Cols & dst, co
     for (uint32_t c = 0; c < src.n; ++c)
         row_bytes += src.width[c];
     KTimer kt(ctx, "group_leaf", 0, 0);
-    k_group_leaf<<<n_leaves, kBuildNT, (size_t)max_cap * 12, ctx->stream>>>(src, dst, leaf_off, lt.meta, lt.cells, lt.next);
+    k_group_leaf<<<n_leaves, kBuildNT, (size_t)max_cap * 16, ctx->stream>>>(src, dst, leaf_off, lt.meta, lt.cells, lt.next);
     PHJ_LAUNCHED(ctx, "group_leaf");
     (void)row_bytes;
     return true;
