@@ -511,6 +511,12 @@ def main():
                 rows_e2e, _ = ctx.run_phj_pure_host(pin[0], pin[1], bits, okeys, oleft, oright)
                 t1 = time.perf_counter()
                 assert rows_e2e == out_rows
+            elif scheme == "phj":
+                # runPhjBep with host buffers: batch uploads, joins and
+                # downloads overlapped inside the call
+                rows_e2e, _ = ctx.run_phj_bep_host(pin[0], pin[1], bits, budget, okeys, oleft, oright)
+                t1 = time.perf_counter()
+                assert rows_e2e == out_rows
             else:
                 tb, tp = ctx.upload(pin[0]), ctx.upload(pin[1])
                 out, _ = run_scheme(ctx, scheme, tb, tp, bits, budget)
@@ -522,8 +528,9 @@ def main():
         e2e_s = dist.max(statistics.mean(e2e_t))
         line["e2e"] = {"value": total_tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                        "ms_per_step": e2e_s * 1e3,
-                       "path": "phj_run_phj_pure_host (pinned host inputs and output columns)" if scheme == "phj-pure"
-                       else "phj_table_upload + scheme + phj_output_download"}
+                       "path": {"phj-pure": "phj_run_phj_pure_host (pinned host inputs and output columns)",
+                                "phj": "phj_run_phj_bep_host (pinned host inputs and output columns)"}.get(
+                                    scheme, "phj_table_upload + scheme + phj_output_download")}
         del pin
 
     # -------- CPU baseline (rank 0, N = 1 only) --------

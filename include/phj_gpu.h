@@ -260,6 +260,18 @@ phj_status phj_run_phj_bep(phj_ctx *ctx, const phj_table *build, const phj_table
                            uint32_t n_passes, uint64_t bep_budget_mib, uint32_t workers, phj_output **out,
                            phj_bep_result *result);
 
+/* runPhjBep with the BlockStreams and the JoinOutput in host memory (pinned
+ * for full speed).  The build side is uploaded whole; the probe side
+ * streams through in batches of at most `bep_budget_mib` MiB and at most
+ * "host_chunk_rows" rows, with the upload of the next batch, the join of
+ * this one and the download of the previous output overlapped (the smaller
+ * batches count more evictions than phj_run_phj_bep with the same budget).
+ * Output and capacity as phj_run_phj_pure_host. */
+phj_status phj_run_phj_bep_host(phj_ctx *ctx, const phj_block_stream *build, const phj_block_stream *probe,
+                                const uint8_t *pass_bits, uint32_t n_passes, uint64_t bep_budget_mib, uint64_t out_capacity,
+                                uint64_t *out_keys, void *const *out_left, void *const *out_right, uint64_t *out_rows,
+                                phj_bep_result *result);
+
 /* Batching (no counterpart in the reference: it runs one join per call).
  * Runs n independent joins in one set of launches (clear, build, lookup,
  * scan, project, each over all n joins through a device work list of

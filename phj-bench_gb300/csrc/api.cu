@@ -1092,6 +1092,264 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
                                           " (the first rows up to the capacity were written)");
 }
 
+
+// PHJ (BEP) with the inputs and the output in host memory.  The build side
+// is uploaded whole, shuffled to full leaf depth and its leaf tables laid
+// out (built on first use, as in run_phj_bep).  The probe side streams
+// through in batches of at most the budget's rows and at most
+// `chunk_rows` (the first a quarter of that, so the first download starts
+// sooner): batch c + 2 uploads on the h2d stream while batch c is
+// scattered, its untouched leaves built, looked up and projected, and the
+// output of batch c - 1 downloads on the d2h stream.  Two device input
+// buffers and per-batch outputs, each reused or freed only after the copy
+// that reads it has finished.
+static void run_phj_bep_host(phj_ctx * ctx, const phj_block_stream & hb, const phj_block_stream & hp, const std::vector<uint32_t> & bits,
+                             uint64_t budget_mib, uint64_t out_cap, uint64_t * out_keys, void * const * out_left, void * const * out_right,
+                             uint64_t * out_rows, phj_bep_result * res, uint64_t chunk_rows)
+{
+    if (!ctx->h2d)
+        PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->h2d, cudaStreamNonBlocking));
+    if (!ctx->d2h)
+        PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->d2h, cudaStreamNonBlocking));
+    begin_run(ctx);
+    Scratch s(ctx);
+    cudaStream_t S = ctx->stream;
+    uint32_t total_bits = 0;
+    for (uint32_t b : bits)
+        total_bits += b;
+    const uint32_t n_leaves = 1u << total_bits;
+    const uint64_t B_rows = hb.total_rows, P_rows = hp.total_rows;
+    const uint64_t row_bytes = 8 + schema_bytes(hp.schema);
+    const uint64_t budget_rows = std::max<uint64_t>(4096, ((budget_mib << 20) / row_bytes) & ~uint64_t(255));
+    const uint64_t C = std::max<uint64_t>(1, std::min<uint64_t>({budget_rows, chunk_rows, std::max<uint64_t>(P_rows, 1)}));
+    const uint64_t C0 = std::max<uint64_t>(1, std::min<uint64_t>(C, std::max<uint64_t>(C / 4, 4096)));
+    auto start = [&](uint64_t c) -> uint64_t { return c == 0 ? 0 : std::min(P_rows, C0 + (c - 1) * C); };
+    const uint64_t n_chunks = P_rows == 0 ? 0 : (P_rows <= C0 ? 1 : 1 + ceil_div(P_rows - C0, C));
+    cudaEvent_t ev[4];
+    for (auto & e : ev)
+        e = take_event(ctx);
+
+    // device buffers, all allocated on the compute stream before any copy
+    phj_table * B = alloc_table(ctx, hb.schema, B_rows);
+    std::unique_ptr<phj_table, std::function<void(phj_table *)>> B_guard(B, [ctx](phj_table * t) { free_table(ctx, t); });
+    Cols in[2];
+    for (auto & c : in)
+        c = alloc_cols_like(s, hp.schema, C);
+    const Cols bpart = alloc_cols_like(s, hb.schema, B_rows);
+    const Cols btmp = alloc_cols_like(s, hb.schema, B_rows);
+    uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
+    const uint32_t p1 = 1u << bits[0];
+    const Cols ppart = alloc_cols_like(s, hp.schema, C);
+    const Cols ptmp = bits[0] > 11 ? alloc_cols_like(s, hp.schema, C) : ppart;
+    uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
+    uint32_t * touched = s.get<uint32_t>((n_leaves + 31) / 32);
+    unsigned long long * ctr = s.get<unsigned long long>(4);
+    uint32_t * heads = s.get<uint32_t>(C);
+    uint32_t * counts = s.get<uint32_t>(probe_chunks(C) + 1);
+    uint32_t * rcnt = s.get<uint32_t>(C);
+    PHJ_CUDA(cudaMemsetAsync(touched, 0, (size_t)((n_leaves + 31) / 32) * 4, S));
+    PHJ_CUDA(cudaMemsetAsync(ctr, 0, 4 * sizeof(unsigned long long), S));
+    PHJ_CUDA(cudaEventRecord(ev[0], S));
+    PHJ_CUDA(cudaStreamWaitEvent(ctx->h2d, ev[0], 0));
+
+    auto upload = [&](const Cols & dst, const phj_block_stream & src, uint64_t r0, uint64_t n) {
+        PHJ_CUDA(cudaMemcpyAsync(dst.keys, src.keys + r0, n * 8, cudaMemcpyHostToDevice, ctx->h2d));
+        for (uint32_t c = 0; c < src.schema.n_payloads; ++c)
+        {
+            const uint32_t w = payload_width(src.schema.types[c]);
+            PHJ_CUDA(cudaMemcpyAsync(dst.col[c], static_cast<const uint8_t *>(src.payloads[c]) + r0 * w, n * w, cudaMemcpyHostToDevice, ctx->h2d));
+        }
+    };
+    std::vector<cudaEvent_t> up(n_chunks), used(n_chunks), proj(n_chunks), down(n_chunks);
+    for (uint64_t c = 0; c < n_chunks; ++c)
+    {
+        up[c] = take_event(ctx);
+        used[c] = take_event(ctx);
+        proj[c] = take_event(ctx);
+        down[c] = take_event(ctx);
+    }
+    const Cols bin = cols_of(*B);
+    if (B_rows)
+        upload(bin, hb, 0, B_rows);
+    cudaEvent_t build_up = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(build_up, ctx->h2d));
+    auto enqueue_chunk = [&](uint64_t c) {
+        if (c >= 2)
+            PHJ_CUDA(cudaStreamWaitEvent(ctx->h2d, used[c - 2], 0));
+        upload(in[c & 1], hp, start(c), start(c + 1) - start(c));
+        PHJ_CUDA(cudaEventRecord(up[c], ctx->h2d));
+    };
+    for (uint64_t c = 0; c < std::min<uint64_t>(2, n_chunks); ++c)
+        enqueue_chunk(c);
+
+    // -------- BUILD SHUFFLE, full leaf depth; tables laid out, built on
+    // first use (src/PHJBep.cpp:128-141) --------
+    PHJ_CUDA(cudaStreamWaitEvent(S, build_up, 0));
+    radix_partition(ctx, s, bin, B_rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    PHJ_CUDA(cudaEventRecord(ev[1], S));
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(B_rows);
+    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt, true);
+    if (ctx->test_stuck_leaf >= 0 && (uint64_t)ctx->test_stuck_leaf < n_leaves)
+    {
+        const uint32_t building = 1;
+        PHJ_CUDA(cudaMemcpyAsync(lt.state + ctx->test_stuck_leaf, &building, sizeof(building), cudaMemcpyHostToDevice, S));
+        PHJ_CUDA(cudaStreamSynchronize(S));
+    }
+    PHJ_CUDA(cudaEventRecord(ev[2], S));
+
+    ProbeArgs a{};
+    a.build = payload_cols(bpart);
+    a.meta = lt.meta;
+    a.cells = lt.cells;
+    a.next = lt.next;
+    a.leaf_bits = total_bits;
+    a.chj = 0;
+    a.any_dup = 0;
+    a.uniform_log2cap = lt.uniform_log2cap;
+    a.row_cnt = rcnt;
+    BepLeaves bl{};
+    bl.state = lt.state;
+    bl.touched = touched;
+    bl.leaf_off = leaf_off;
+    bl.build_keys = bpart.keys;
+    bl.meta = lt.meta;
+    bl.cells = lt.cells;
+    bl.next = lt.next;
+    bl.leaf_bits = total_bits;
+    bl.n_leaves = n_leaves;
+    bl.smem_cells = (uint32_t)std::min<uint64_t>(lt.uniform_log2cap >= 0 ? (1ull << lt.uniform_log2cap) : bit_ceil64(2ull * std::max<uint32_t>(lt.max_rows, 1)),
+                                                 8192);
+    bl.wait_limit_ns = (uint64_t)ctx->wait_limit_ms * 1000000ull;
+    bl.ctr = ctr;
+    bl.queue = s.get<uint32_t>(n_leaves);
+    bl.queue_len = s.get<uint32_t>(2);
+    bl.any_dup = s.get<int>(1);
+    PHJ_CUDA(cudaMemsetAsync(bl.any_dup, 0, sizeof(int), S));
+
+    // -------- PROBE, batch by batch --------
+    std::vector<phj_output *> outs(n_chunks, nullptr);
+    uint64_t total = 0, copied = 0, peak_rows = 0;
+    float t_shuffle = 0.f, t_lazy = 0.f, t_probe = 0.f;
+    cudaEvent_t c0 = take_event(ctx), c1 = take_event(ctx), c2 = take_event(ctx), c3 = take_event(ctx);
+    try
+    {
+        for (uint64_t c = 0; c < n_chunks; ++c)
+        {
+            const uint64_t n = start(c + 1) - start(c);
+            peak_rows = std::max(peak_rows, n);
+            Scratch sc(ctx);
+            PHJ_CUDA(cudaStreamWaitEvent(S, up[c], 0));
+            PHJ_CUDA(cudaEventRecord(c0, S));
+            // the batch's first radix pass also flags the leaves its rows
+            // touch (its histogram reads every key once anyway)
+            ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
+            try
+            {
+                radix_partition(ctx, sc, in[c & 1], n, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            }
+            catch (...)
+            {
+                ctx->leaf_mark = LeafMark{};
+                throw;
+            }
+            ctx->leaf_mark = LeafMark{};
+            PHJ_CUDA(cudaEventRecord(used[c], S)); // the input buffer is free again
+            k_count_nonempty<<<(unsigned)ceil_div(p1, 256), 256, 0, S>>>(poff, p1, ctr + 3);
+            PHJ_LAUNCHED(ctx, "count_refinements");
+            PHJ_CUDA(cudaEventRecord(c1, S));
+            a.probe = ppart;
+            a.probe_rows = n;
+            // lazy build of the leaves this batch touches
+            a.any_dup = bep_build_touched(ctx, bl) ? 1 : 0;
+            check_device_error(ctx);
+            PHJ_CUDA(cudaEventRecord(c2, S));
+            const uint64_t rows = probe_lookup(ctx, sc, a, heads, counts);
+            phj_output * o = new_output(ctx, hb.schema, hp.schema, rows);
+            outs[c] = o;
+            o->rows = rows;
+            probe_project(ctx, a, o, 0, heads, counts, rows);
+            PHJ_CUDA(cudaEventRecord(proj[c], S));
+            if (c + 2 < n_chunks)
+                enqueue_chunk(c + 2);
+            // download into the host columns at the running offset
+            PHJ_CUDA(cudaStreamWaitEvent(ctx->d2h, proj[c], 0));
+            const uint64_t keep = copied < out_cap ? std::min<uint64_t>(rows, out_cap - copied) : 0;
+            if (keep)
+            {
+                PHJ_CUDA(cudaMemcpyAsync(out_keys + copied, o->keys, keep * 8, cudaMemcpyDeviceToHost, ctx->d2h));
+                for (uint32_t k = 0; k < hb.schema.n_payloads; ++k)
+                {
+                    const uint32_t w = payload_width(hb.schema.types[k]);
+                    PHJ_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(out_left[k]) + copied * w, o->lcol[k], keep * w, cudaMemcpyDeviceToHost, ctx->d2h));
+                }
+                for (uint32_t k = 0; k < hp.schema.n_payloads; ++k)
+                {
+                    const uint32_t w = payload_width(hp.schema.types[k]);
+                    PHJ_CUDA(cudaMemcpyAsync(static_cast<uint8_t *>(out_right[k]) + copied * w, o->rcol[k], keep * w, cudaMemcpyDeviceToHost, ctx->d2h));
+                }
+            }
+            copied += keep;
+            PHJ_CUDA(cudaEventRecord(down[c], ctx->d2h));
+            total += rows;
+            // free the output two batches back once its download is done
+            if (c >= 2 && outs[c - 2])
+            {
+                PHJ_CUDA(cudaStreamWaitEvent(S, down[c - 2], 0));
+                free_output(ctx, outs[c - 2]);
+                outs[c - 2] = nullptr;
+            }
+            PHJ_CUDA(cudaEventRecord(c3, S));
+            PHJ_CUDA(cudaEventSynchronize(c3));
+            t_shuffle += event_ms(c0, c1);
+            t_lazy += event_ms(c1, c2);
+            t_probe += event_ms(c2, c3);
+        }
+        if (n_chunks)
+            PHJ_CUDA(cudaStreamWaitEvent(S, down[n_chunks - 1], 0));
+        for (auto & o : outs)
+            if (o)
+            {
+                free_output(ctx, o);
+                o = nullptr;
+            }
+        PHJ_CUDA(cudaEventRecord(ev[3], S));
+        PHJ_CUDA(cudaEventSynchronize(ev[3]));
+        check_device_error(ctx);
+    }
+    catch (...)
+    {
+        cudaStreamSynchronize(ctx->h2d);
+        cudaStreamSynchronize(ctx->d2h);
+        for (auto & o : outs)
+            free_output(ctx, o);
+        throw;
+    }
+    if (out_rows)
+        *out_rows = total;
+    if (res)
+    {
+        unsigned long long cv[4] = {};
+        read_small(ctx, {{cv, ctr, sizeof(cv)}});
+        const float bs = event_ms(ev[0], ev[1]), bd = event_ms(ev[1], ev[2]) + t_lazy, e2e = event_ms(ev[0], ev[3]);
+        fill_phase(res->build_shuffle, bs, B_rows);
+        fill_phase(res->build, bd, B_rows);
+        fill_phase(res->probe_shuffle, t_shuffle, P_rows);
+        fill_phase(res->probe, t_probe, P_rows);
+        fill_phase(res->eviction_overhead, std::max(0.f, e2e - bs - bd - t_shuffle - t_probe), P_rows);
+        res->e2e_wall_ms = e2e;
+        res->peak_mem_bytes = ctx->peak_bytes;
+        res->bep_budget_mib = budget_mib;
+        res->bep_evictions = cv[2];
+        res->bep_refinements = cv[3];
+        res->bep_peak_bytes = peak_rows * row_bytes;
+        res->bep_build_skip_retries = cv[1];
+    }
+    if (total > out_cap)
+        throw Error(PHJ_ERR_CAPACITY, "host output holds " + std::to_string(out_cap) + " rows; the join has " + std::to_string(total) +
+                                          " (the first rows up to the capacity were written)");
+}
+
 } // namespace phjg
 
 using namespace phjg;
@@ -1524,6 +1782,42 @@ phj_status phj_run_phj_pure_host(phj_ctx * ctx, const phj_block_stream * build, 
             if ((probe->total_rows && !probe->payloads[c]) || (out_capacity && (!out_right || !out_right[c])))
                 throw Error(PHJ_ERR_INVALID_ARGUMENT, "null probe payload column");
         run_phj_pure_host(ctx, *build, *probe, bits, out_capacity, out_keys, out_left, out_right, out_rows, result, (uint64_t)ctx->host_chunk_rows);
+    });
+}
+
+phj_status phj_run_phj_bep_host(phj_ctx * ctx, const phj_block_stream * build, const phj_block_stream * probe, const uint8_t * pass_bits,
+                                uint32_t n_passes, uint64_t bep_budget_mib, uint64_t out_capacity, uint64_t * out_keys, void * const * out_left,
+                                void * const * out_right, uint64_t * out_rows, phj_bep_result * result)
+{
+    if (!ctx || !build || !probe)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    if (out_rows)
+        *out_rows = 0;
+    return guard(ctx, [&] {
+        const std::vector<uint32_t> bits = check_bits(pass_bits, n_passes);
+        check_schema(build->schema, "build stream");
+        check_schema(probe->schema, "probe stream");
+        if (build->location != PHJ_HOST || probe->location != PHJ_HOST)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "phj_run_phj_bep_host takes host streams");
+        if (build->total_rows >= (1ull << 31) || probe->total_rows >= (1ull << 32))
+            throw Error(PHJ_ERR_UNSUPPORTED, "device schemes support < 2^31 build rows and < 2^32 probe rows");
+        uint32_t total_bits = 0;
+        for (uint32_t b : bits)
+            total_bits += b;
+        if (total_bits > 20)
+            throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) on the device takes at most 20 radix bits (2^20 leaves)");
+        if ((build->total_rows && !build->keys) || (probe->total_rows && !probe->keys))
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "null key column");
+        if (out_capacity && !out_keys)
+            throw Error(PHJ_ERR_INVALID_ARGUMENT, "null output key column");
+        for (uint32_t c = 0; c < build->schema.n_payloads; ++c)
+            if ((build->total_rows && !build->payloads[c]) || (out_capacity && (!out_left || !out_left[c])))
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "null build payload column");
+        for (uint32_t c = 0; c < probe->schema.n_payloads; ++c)
+            if ((probe->total_rows && !probe->payloads[c]) || (out_capacity && (!out_right || !out_right[c])))
+                throw Error(PHJ_ERR_INVALID_ARGUMENT, "null probe payload column");
+        run_phj_bep_host(ctx, *build, *probe, bits, bep_budget_mib, out_capacity, out_keys, out_left, out_right, out_rows, result,
+                         (uint64_t)ctx->host_chunk_rows);
     });
 }
 

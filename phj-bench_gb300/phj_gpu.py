@@ -144,6 +144,9 @@ def load() -> C.CDLL:
         "phj_run_phj_pure_host": (C.c_int, [P, C.POINTER(BlockStreamDesc), C.POINTER(BlockStreamDesc), C.POINTER(C.c_uint8), C.c_uint32,
                                             C.c_uint64, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
                                             C.POINTER(PhjResultC)]),
+        "phj_run_phj_bep_host": (C.c_int, [P, C.POINTER(BlockStreamDesc), C.POINTER(BlockStreamDesc), C.POINTER(C.c_uint8), C.c_uint32,
+                                           C.c_uint64, C.c_uint64, P, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p), C.POINTER(C.c_uint64),
+                                           C.POINTER(BepResultC)]),
         "phj_run_phj_bep": (C.c_int, [P, P, P, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint64, C.c_uint32, C.POINTER(P),
                                       C.POINTER(BepResultC)]),
         "phj_autotune_radix": (C.c_int, [C.c_uint64, C.c_uint64, C.POINTER(C.c_uint8), C.POINTER(C.c_uint32)]),
@@ -411,6 +414,20 @@ class Context:
         r = PhjResultC()
         self._check(self.lib.phj_run_phj_pure_host(self.ptr, C.byref(db), C.byref(dp), bits, len(pass_bits), len(out_keys),
                                                    out_keys.ctypes.data, lp, rp, C.byref(rows), C.byref(r)))
+        return rows.value, r
+
+    def run_phj_bep_host(self, build: BlockStream, probe: BlockStream, pass_bits: Sequence[int], budget_mib: int, out_keys: np.ndarray,
+                         out_left: Sequence[np.ndarray], out_right: Sequence[np.ndarray]):
+        """phj_run_phj_bep_host: host inputs, host output columns (pinned
+        for full speed).  Returns (output rows, BepResultC)."""
+        db, dp = self._desc(build), self._desc(probe)
+        bits = (C.c_uint8 * max(1, len(pass_bits)))(*pass_bits)
+        lp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_left])
+        rp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_right])
+        rows = C.c_uint64()
+        r = BepResultC()
+        self._check(self.lib.phj_run_phj_bep_host(self.ptr, C.byref(db), C.byref(dp), bits, len(pass_bits), budget_mib, len(out_keys),
+                                                  out_keys.ctypes.data, lp, rp, C.byref(rows), C.byref(r)))
         return rows.value, r
 
     def upload(self, s: BlockStream) -> Table:

@@ -326,3 +326,42 @@ def test_packed_build_payloads(ctx, pack, build_types):
         assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
     finally:
         ctx.set_int("pack_build", 1)
+
+
+@pytest.mark.parametrize("name", ["c2_mini", "c3_mini", "edge", "empty_probe", "empty_build", "no_match"])
+@pytest.mark.parametrize("chunk,budget", [(4096, 1), (1 << 24, 1), (1 << 24, 512)])
+def test_host_buffer_phj_bep(ctx, name, chunk, budget):
+    # runPhjBep with host inputs and outputs: batches of at most the budget
+    # and at most host_chunk_rows rows, uploads / joins / downloads
+    # overlapped; the rows must equal the oracle's
+    b, p = cases.make(name)
+    expected = O.join_rows(b, p)
+    bits = cases.BITS[name]
+    ctx.set_int("host_chunk_rows", chunk)
+    try:
+        keys, left, right = host_out(ctx, b, p, len(expected) + 5, pinned=(chunk == 4096))
+        rows, res = ctx.run_phj_bep_host(b, p, bits, budget, keys, left, right)
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
+    assert rows == len(expected)
+    jo = P.JoinOutput(b.types, p.types, keys[:rows], [c[:rows] for c in left], [c[:rows] for c in right])
+    assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
+    assert res.e2e_wall_ms > 0 and res.bep_budget_mib == budget
+    if p.total_rows and b.total_rows:
+        assert res.bep_evictions > 0 and res.bep_refinements > 0
+
+
+def test_host_buffer_phj_bep_short_capacity(ctx):
+    b, p = cases.make("c2_mini")
+    expected = O.join_rows(b, p)
+    ctx.set_int("host_chunk_rows", 8192)
+    try:
+        keys, left, right = host_out(ctx, b, p, 1000)
+        with pytest.raises(P.PhjError) as e:
+            ctx.run_phj_bep_host(b, p, [4, 4], 1, keys, left, right)
+        assert e.value.status == 7
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
+    keys, left, right = host_out(ctx, b, p, len(expected))
+    rows, _ = ctx.run_phj_bep_host(b, p, [4, 4], 1, keys, left, right)
+    assert rows == len(expected)
