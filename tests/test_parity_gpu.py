@@ -365,3 +365,29 @@ def test_host_buffer_phj_bep_short_capacity(ctx):
     keys, left, right = host_out(ctx, b, p, len(expected))
     rows, _ = ctx.run_phj_bep_host(b, p, [4, 4], 1, keys, left, right)
     assert rows == len(expected)
+
+
+def test_host_buffer_bep_stuck_leaf_times_out_and_context_recovers(ctx):
+    # The same bounded-wait failure through the host-buffer entry point:
+    # the error comes back with the upload / download streams drained, and
+    # the context runs the next host-buffer join.
+    b, p = cases.make("c2_mini")
+    expected = O.join_rows(b, p)
+    keys, left, right = host_out(ctx, b, p, len(expected))
+    ctx.set_int("wait_limit_ms", 100)
+    ctx.set_int("test_stuck_leaf", 3)
+    ctx.set_int("host_chunk_rows", 8192)
+    try:
+        with pytest.raises(P.PhjError) as e:
+            ctx.run_phj_bep_host(b, p, [4], 1, keys, left, right)
+        assert e.value.status == P.ERR_DEVICE_TIMEOUT
+    finally:
+        ctx.set_int("test_stuck_leaf", -1)
+        ctx.set_int("wait_limit_ms", 1000)
+    try:
+        rows, _ = ctx.run_phj_bep_host(b, p, [4], 1, keys, left, right)
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
+    assert rows == len(expected)
+    jo = P.JoinOutput(b.types, p.types, keys[:rows], [c[:rows] for c in left], [c[:rows] for c in right])
+    assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
