@@ -1,6 +1,7 @@
-// cpu_port.cpp -- C++ restatement of the reference's CPU PHJ-PURE and CHJ
-// schemes for timing where the reference cannot be compiled.  BASELINE
-// INFRASTRUCTURE ONLY.  See cpu_port.h for the reference file:line map.
+// cpu_port.cpp -- C++ restatement of the reference's CPU CHJ, PHJ-PURE and
+// PHJ (BEP) schemes, timed as the CPU baseline where the reference cannot be
+// compiled.  Test and measurement infrastructure only, never on the device
+// path.  See cpu_port.h for the reference file:line map.
 #include "cpu_port.h"
 
 #include <algorithm>
