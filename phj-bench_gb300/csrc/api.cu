@@ -514,6 +514,33 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     *out = o;
 }
 
+// Bits of the probe side's first (and only written) radix pass in PHJ-PURE.
+// The lookup takes every row's leaf from the whole hash, so this width is a
+// performance choice, not the configuration's: buckets narrow enough that
+// one bucket's leaf tables and build payloads stay in L2 while its rows are
+// probed, and otherwise as wide as possible (fewer buckets: longer runs per
+// bucket in the scatter's tiles).  The working set is estimated before the
+// tables exist (the pass runs beside the build side): cells at the load
+// factor with up to 2x for power-of-two and uniform sizing, the next-chain
+// and the payloads; the widest buckets whose share stays within a fifth of
+// L2 are taken (16M x 256M: 6 bits, 6.83 ms against 7.12 ms at the
+// configuration's 8 and 7.35 ms at 5).  "probe_pass_bits" overrides it.
+static uint32_t probe_pass_bits(const phj_ctx * ctx, const std::vector<uint32_t> & bits, const phj_table & build)
+{
+    uint32_t total = 0;
+    for (uint32_t b : bits)
+        total += b;
+    const uint32_t most = std::min<uint32_t>(total, 11);
+    if (ctx->probe_pass_bits)
+        return std::min<uint32_t>(ctx->probe_pass_bits, most);
+    const uint64_t ws = build.rows * (16ull * ctx->table_cap_pct / 100 * 2 + 8 + schema_bytes(build.schema));
+    const uint64_t target = std::max<uint64_t>(ctx->l2_bytes / 5, 1);
+    uint32_t b = 1;
+    while (b < most && (ws >> b) > target)
+        ++b;
+    return b;
+}
+
 static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P, const std::vector<uint32_t> & bits, phj_output ** out,
                          phj_phj_result * res)
 {
@@ -550,10 +577,11 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
         try
         {
             PHJ_CUDA(cudaEventRecord(ev[5], ctx->stream));
+            const uint32_t pb = probe_pass_bits(ctx, bits, B);
             const Cols ppart = alloc_cols_like(s, P.schema, P.rows);
-            const bool split = bits[0] > 11;
+            const bool split = pb > 11;
             const Cols ptmp = split ? alloc_cols_like(s, P.schema, P.rows) : ppart;
-            uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
+            uint32_t * poff = s.get<uint32_t>((1ull << pb) + 1);
             // a two-stage ring leaves shared memory on each SM for the build
             // side's kernels running beside this pass (unless pinned)
             const uint32_t pinned_stages = ctx->p1_stages;
@@ -561,7 +589,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
                 ctx->p1_stages = 2;
             try
             {
-                radix_partition(ctx, s, a.probe, P.rows, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+                radix_partition(ctx, s, a.probe, P.rows, {pb}, ppart, ptmp, poff, "probe_scatter");
             }
             catch (...)
             {
@@ -976,8 +1004,9 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     // packing them would only add to the time before the first download)
     const bool mat = materialize_probe(ctx, lt, *B, n_leaves) && P_rows > 0;
     const Cols ppart = mat ? alloc_cols_like(s, hp.schema, C) : Cols{};
-    const Cols ptmp = mat && bits[0] > 11 ? alloc_cols_like(s, hp.schema, C) : ppart;
-    uint32_t * poff = s.get<uint32_t>((1ull << bits[0]) + 1);
+    const uint32_t pb = probe_pass_bits(ctx, bits, *B);
+    const Cols ptmp = mat && pb > 11 ? alloc_cols_like(s, hp.schema, C) : ppart;
+    uint32_t * poff = s.get<uint32_t>((1ull << pb) + 1);
     uint32_t * heads = s.get<uint32_t>(C);
     uint32_t * counts = s.get<uint32_t>(probe_chunks(C) + 1);
     if (grouped || lt.any_dup)
@@ -999,7 +1028,7 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
             a.probe = in[c & 1];
             if (mat)
             {
-                radix_partition(ctx, sc, in[c & 1], n, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+                radix_partition(ctx, sc, in[c & 1], n, {pb}, ppart, ptmp, poff, "probe_scatter");
                 a.probe = ppart;
                 PHJ_CUDA(cudaEventRecord(used[c], S)); // the input buffer is free again
             }
@@ -1476,6 +1505,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->p1_stages = (uint32_t)value;
     else if (std::strcmp(name, "pack_build") == 0 && (value == 0 || value == 1))
         ctx->pack_build = (int)value;
+    else if (std::strcmp(name, "probe_pass_bits") == 0 && value >= 0 && value <= 11)
+        ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
     else
@@ -1503,6 +1534,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->p1_stages;
     else if (std::strcmp(name, "pack_build") == 0)
         *value = ctx->pack_build;
+    else if (std::strcmp(name, "probe_pass_bits") == 0)
+        *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
     else if (std::strcmp(name, "device") == 0)

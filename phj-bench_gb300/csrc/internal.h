@@ -106,6 +106,7 @@ struct phj_ctx
     uint32_t p1_tile_rows = 0;    // first radix pass: rows per staged tile (0: chosen per row width)
     uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
     int pack_build = 1;           // pack unique-key build payloads row-major for the projection (0: columns)
+    uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
     LeafMark leaf_mark;           // consumed by the next first radix pass
