@@ -166,9 +166,10 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        row) for CHJ and PHJ-PURE joins without repeated build keys whose
  *        2+ build payload columns fit 16 bytes, so the projection gathers one
  *        value per output row; 0 gathers column by column;
- *   "probe_pass_bits": bits of the radix pass PHJ-PURE writes out for the
- *        probe side, 1..11, 0 (default) chosen from the build side's size so
- *        one bucket's leaf tables stay in L2;
+ *   "probe_pass_bits": bits of the radix pass written out for the probe
+ *        side, 1..11; 0 (default): PHJ-PURE chooses them from the build
+ *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's
+ *        batches take the configuration's first pass;
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
  *        leaf BUILDING before the probe, so its waits run out. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);

@@ -703,10 +703,13 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     const uint64_t row_bytes = 8 + schema_bytes(P.schema);
     const uint64_t budget_rows = (budget_mib << 20) / row_bytes;
     const uint64_t batch_rows = std::min<uint64_t>(std::max<uint64_t>(P.rows, 1), std::max<uint64_t>(4096, budget_rows & ~uint64_t(255)));
-    const uint32_t p1 = 1u << bits[0];
+    // the probe batches' written pass: the configuration's first pass, or
+    // the "probe_pass_bits" option
+    const uint32_t pb = ctx->probe_pass_bits ? std::min<uint32_t>(ctx->probe_pass_bits, std::min<uint32_t>(total_bits, 11)) : bits[0];
+    const uint32_t p1 = 1u << pb;
     const Cols pin = cols_of(P);
     const Cols ppart = alloc_cols_like(s, P.schema, batch_rows);
-    const Cols ptmp = bits[0] > 11 ? alloc_cols_like(s, P.schema, batch_rows) : ppart;
+    const Cols ptmp = pb > 11 ? alloc_cols_like(s, P.schema, batch_rows) : ppart;
     uint32_t * poff = s.get<uint32_t>((uint64_t)p1 + 1);
     uint32_t * touched = s.get<uint32_t>((n_leaves + 31) / 32);
     PHJ_CUDA(cudaMemsetAsync(touched, 0, (size_t)((n_leaves + 31) / 32) * 4, ctx->stream));
@@ -744,7 +747,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
             ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
             if (!pinned_stages)
                 ctx->p1_stages = 2;
-            radix_partition(ctx, s, pin, std::min(batch_rows, P.rows), {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+            radix_partition(ctx, s, pin, std::min(batch_rows, P.rows), {pb}, ppart, ptmp, poff, "probe_scatter");
             ctx->p1_stages = pinned_stages;
             ctx->leaf_mark = LeafMark{};
             PHJ_CUDA(cudaEventRecord(es[1], ctx->stream));
@@ -840,7 +843,7 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
                 // the batch's first radix pass also flags the leaves its
                 // rows touch (its histogram reads every key once anyway)
                 ctx->leaf_mark = LeafMark{touched, 64u - total_bits, (n_leaves + 31) / 32};
-                radix_partition(ctx, sb, cols_from(pin, r0), n_b, {bits[0]}, ppart, ptmp, poff, "probe_scatter");
+                radix_partition(ctx, sb, cols_from(pin, r0), n_b, {pb}, ppart, ptmp, poff, "probe_scatter");
                 ctx->leaf_mark = LeafMark{};
             }
             k_count_nonempty<<<(unsigned)ceil_div(p1, 256), 256, 0, ctx->stream>>>(poff, p1, ctr + 3);
