@@ -550,7 +550,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     for (uint32_t b : bits)
         total_bits += b;
     const uint32_t n_leaves = 1u << total_bits;
-    cudaEvent_t ev[7];
+    cudaEvent_t ev[9];
     for (auto & e : ev)
         e = take_event(ctx);
     PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
@@ -615,17 +615,34 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
     uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
     LeafTables lt;
-    bool grouped = false;
+    bool grouped = false, packing = false;
     try
     {
         radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
         PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
 
-        // build payloads packed for the projection, ahead of the tables
-        // (beside the probe side's first pass); dropped if a key repeats
+        // build payloads packed for the projection on a third stream,
+        // beside the leaf tables (both only read the partitioned rows);
+        // dropped if a key repeats
         a.build = payload_cols(bpart);
         a.any_dup = 0;
-        pack_build_payloads(ctx, s, a, B.rows);
+        if (!ctx->aux)
+            PHJ_CUDA(cudaStreamCreateWithFlags(&ctx->aux, cudaStreamNonBlocking));
+        PHJ_CUDA(cudaEventRecord(ev[7], ctx->stream));
+        PHJ_CUDA(cudaStreamWaitEvent(ctx->aux, ev[7], 0));
+        ctx->stream = ctx->aux;
+        try
+        {
+            pack_build_payloads(ctx, s, a, B.rows);
+        }
+        catch (...)
+        {
+            ctx->stream = main_stream;
+            throw;
+        }
+        PHJ_CUDA(cudaEventRecord(ev[8], ctx->stream));
+        ctx->stream = main_stream;
+        packing = true;
 
         // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
         lt.next = s.get<uint64_t>(B.rows);
@@ -641,10 +658,13 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     {
         if (mat)
             cudaStreamSynchronize(ctx->side); // its buffers are freed with the scratch
+        if (packing)
+            cudaStreamSynchronize(ctx->aux);
         throw;
     }
     if (mat)
         PHJ_CUDA(cudaStreamWaitEvent(ctx->stream, ev[6], 0));
+    PHJ_CUDA(cudaStreamWaitEvent(ctx->stream, ev[8], 0));
     PHJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
 
     // -------- PROBE with projection (src/PHJ.cpp:284-299) --------
@@ -1475,6 +1495,8 @@ void phj_ctx_destroy(phj_ctx * ctx)
         cudaStreamDestroy(ctx->d2h);
     if (ctx->side)
         cudaStreamDestroy(ctx->side);
+    if (ctx->aux)
+        cudaStreamDestroy(ctx->aux);
     delete ctx;
 }
 

@@ -82,6 +82,7 @@ struct phj_ctx
     cudaStream_t stream = nullptr;
     cudaStream_t h2d = nullptr, d2h = nullptr; // copy streams of the host-buffer entry points (made on first use)
     cudaStream_t side = nullptr;               // second compute stream: probe-side first pass beside the build
+    cudaStream_t aux = nullptr;                // third compute stream: build payload packing beside the leaf tables
     cudaMemPool_t pool = nullptr;
     std::string last_error;
     uint64_t launches = 0;

@@ -845,7 +845,8 @@ void pack_build_payloads(phj_ctx * ctx, Scratch & s, ProbeArgs & a, uint64_t bui
     uint4 * p = s.get<uint4>(build_rows);
     {
         KTimer kt(ctx, "pack_build", build_rows, build_rows * (off + 16));
-        k_pack_rows<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(build_rows, 256), (uint64_t)ctx->num_sms * 8)), 256, 0, ctx->stream>>>(
+        // two CTAs per SM: the leaf-table build runs beside it
+        k_pack_rows<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(build_rows, 256), (uint64_t)ctx->num_sms * 2)), 256, 0, ctx->stream>>>(
             a.build, build_rows, pk, p);
         PHJ_LAUNCHED(ctx, "pack_build");
     }

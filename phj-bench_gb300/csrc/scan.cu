@@ -1,13 +1,15 @@
 // scan.cu -- exclusive prefix sum over u32 arrays (histogram matrices, leaf
-// sizes, table capacities).  Reduce-then-scan: each 1024-thread block owns
-// 8192 consecutive values; block sums are scanned recursively.
+// sizes, table capacities).  Reduce-then-scan: each 512-thread block owns
+// 4096 consecutive values; block sums are scanned recursively.  512 threads
+// (14K registers) fit on an SM beside a first-pass scatter CTA, so the build
+// side's scans do not wait for the probe side's pass to retire.
 #include "internal.h"
 
 namespace phjg
 {
 namespace
 {
-constexpr int kScanNT = 1024;
+constexpr int kScanNT = 512;
 constexpr int kScanPerThread = 8;
 constexpr uint64_t kScanTile = (uint64_t)kScanNT * kScanPerThread;
 
@@ -29,7 +31,7 @@ __global__ void __launch_bounds__(kScanNT) k_scan_reduce(const uint32_t * __rest
         sums[blockIdx.x] = total;
 }
 
-// Scans one tile of 8192 values; thread t owns 8 consecutive values.  Adds
+// Scans one tile of 4096 values; thread t owns 8 consecutive values.  Adds
 // `carry[blockIdx.x]` (when given) and writes total to out[m] from the last
 // tile.  In-place (in == out) is allowed.
 __global__ void __launch_bounds__(kScanNT) k_scan_tile(const uint32_t * in, uint64_t m, const uint32_t * __restrict__ carry, uint32_t * out)
