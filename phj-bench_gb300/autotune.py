@@ -3,8 +3,8 @@
 For a (build, probe) pair resident on the device it times candidate
 configurations of one scheme and keeps the fastest: radix bits and pass
 count, leaf-table load factor (table_cap_pct), the first radix pass's tile
-rows and bulk-copy ring depth, and whether the probe side's first pass is
-written out.  The search is coordinate descent from the heuristic start
+rows and bulk-copy ring depth, whether the probe side's pass is written
+out, and its width (probe_pass_bits).  The search is coordinate descent from the heuristic start
 (phj_autotune_radix): each knob in turn is swept with the others held, and
 the best value is kept.  Results are cached per (scheme, log2 build rows,
 log2 probe rows, build/probe row widths) in a JSON file, so a later join of
@@ -24,7 +24,7 @@ from typing import Dict, List, Optional, Sequence
 
 import phj_gpu as P
 
-KNOBS = ("pass_bits", "table_cap_pct", "p1_tile_rows", "p1_stages", "probe_materialize")
+KNOBS = ("pass_bits", "table_cap_pct", "p1_tile_rows", "p1_stages", "probe_materialize", "probe_pass_bits")
 DEFAULT_CACHE = os.path.join(os.path.expanduser("~"), ".cache", "phj_gb300_tune.json")
 
 
@@ -62,17 +62,18 @@ def knob_values(build_rows: int) -> Dict[str, list]:
         "p1_tile_rows": [0, 4096, 2048, 1024],
         "p1_stages": [0, 2, 3, 4],
         "probe_materialize": [-1, 1, 0],
+        "probe_pass_bits": [0, 5, 6, 7, 8],
     }
 
 
 def apply(ctx: "P.Context", cfg: dict) -> None:
-    for k in ("table_cap_pct", "p1_tile_rows", "p1_stages", "probe_materialize"):
+    for k in ("table_cap_pct", "p1_tile_rows", "p1_stages", "probe_materialize", "probe_pass_bits"):
         if k in cfg:
             ctx.set_int(k, int(cfg[k]))
 
 
 def reset(ctx: "P.Context") -> None:
-    apply(ctx, {"table_cap_pct": 200, "p1_tile_rows": 0, "p1_stages": 0, "probe_materialize": -1})
+    apply(ctx, {"table_cap_pct": 200, "p1_tile_rows": 0, "p1_stages": 0, "probe_materialize": -1, "probe_pass_bits": 0})
 
 
 def _time(ctx, scheme, b, p, cfg, reps, budget_mib):
@@ -96,7 +97,7 @@ def tune(ctx: "P.Context", build: "P.Table", probe: "P.Table", scheme: str = "ph
          cache_path: Optional[str] = DEFAULT_CACHE, use_cache: bool = True, log=None) -> dict:
     """Returns the fastest configuration found (and applies its context
     options to `ctx`): {"pass_bits", "table_cap_pct", "p1_tile_rows",
-    "p1_stages", "probe_materialize", "ms", "trials"}."""
+    "p1_stages", "probe_materialize", "probe_pass_bits", "ms", "trials"}."""
     key = shape_key(scheme, build.rows, probe.rows, build.types, probe.types)
     cache = {}
     if cache_path and use_cache and os.path.exists(cache_path):
@@ -109,7 +110,7 @@ def tune(ctx: "P.Context", build: "P.Table", probe: "P.Table", scheme: str = "ph
             return dict(cache[key], cached=True)
     values = knob_values(build.rows)
     best = {"pass_bits": P.autotune_radix(build.rows), "table_cap_pct": 200, "p1_tile_rows": 0, "p1_stages": 0,
-            "probe_materialize": -1}
+            "probe_materialize": -1, "probe_pass_bits": 0}
     best_ms, ref_fp = _time(ctx, scheme, build, probe, best, reps, budget_mib)
     trials = 1
     for knob in KNOBS:
