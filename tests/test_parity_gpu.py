@@ -391,3 +391,36 @@ def test_host_buffer_bep_stuck_leaf_times_out_and_context_recovers(ctx):
     assert rows == len(expected)
     jo = P.JoinOutput(b.types, p.types, keys[:rows], [c[:rows] for c in left], [c[:rows] for c in right])
     assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
+
+
+@pytest.mark.parametrize("pb", [1, 6, 11])
+def test_probe_pass_width_override(ctx, pb):
+    # The probe side's written pass width is a performance choice: any
+    # width gives the same rows (the lookup takes the leaf from the whole
+    # hash), including one wider than the configuration's first pass.
+    b, p = cases.make("c2_mini")
+    ctx.set_int("probe_pass_bits", pb)
+    try:
+        for bits in ([4, 4], [3], [6, 5]):
+            jo, fp, _ = run(ctx, "phj-pure", b, p, bits, 1)
+            check(b, p, jo, fp)
+            jo, fp, _ = run(ctx, "phj", b, p, bits)
+            check(b, p, jo, fp)
+    finally:
+        ctx.set_int("probe_pass_bits", 0)
+
+
+def test_chj_irregular_blocks_with_packed_payloads(ctx):
+    # CHJ's build rows are (input block, row); the packed payload rows are
+    # indexed by the global row the block offsets give.
+    bk = G.gen_keys(0, 3000, 41, 4)
+    sizes = np.array([5, 1200, 1, 794, 1000], dtype=np.uint32)
+    b = P.BlockStream([P.U32, P.U16, P.U8], bk, G.payload_columns(42, [P.U32, P.U16, P.U8], 3000), block_rows=sizes)
+    p = P.BlockStream([P.U64], G.gen_keys(4, 9000, 43, 4, domain=3000, match_permille=900), G.payload_columns(44, [P.U64], 9000))
+    for pack in (1, 0):
+        ctx.set_int("pack_build", pack)
+        try:
+            jo, fp, _ = run(ctx, "chj", b, p)
+            check(b, p, jo, fp)
+        finally:
+            ctx.set_int("pack_build", 1)
