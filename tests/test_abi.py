@@ -102,3 +102,31 @@ def test_serve_rejects_bad_config_and_needs_a_device(lib):
                                        (64 << 20, [9, 9]), (1 << 31, [8, 8, 7])])
 def test_autotune_radix_leaf_target(lib, rows, want):
     assert P.autotune_radix(rows) == want
+
+
+def test_entry_points_reject_a_null_context_without_a_device(lib):
+    # Every join entry point checks its handles before any CUDA call, so a
+    # missing context is PHJ_ERR_INVALID_ARGUMENT here as on a GPU machine.
+    out = ctypes.c_void_p()
+    desc = P.BlockStreamDesc()
+    rows = ctypes.c_uint64()
+    keys = (ctypes.c_uint64 * 1)()
+    ptrs = (ctypes.c_void_p * 1)()
+    calls = {
+        "phj_run_chj": lambda: lib.phj_run_chj(None, None, None, ctypes.byref(out), None),
+        "phj_run_phj_pure": lambda: lib.phj_run_phj_pure(None, None, None, None, 0, ctypes.byref(out), None),
+        "phj_run_phj_bep": lambda: lib.phj_run_phj_bep(None, None, None, None, 0, 0, 0, ctypes.byref(out), None),
+        "phj_run_phj_pure_host": lambda: lib.phj_run_phj_pure_host(None, ctypes.byref(desc), ctypes.byref(desc), None, 0, 1,
+                                                                   keys, ptrs, ptrs, ctypes.byref(rows), None),
+        "phj_run_phj_bep_host": lambda: lib.phj_run_phj_bep_host(None, ctypes.byref(desc), ctypes.byref(desc), None, 0, 0, 1,
+                                                                 keys, ptrs, ptrs, ctypes.byref(rows), None),
+        "phj_run_chj_noalloc": lambda: lib.phj_run_chj_noalloc(None, None, None, 0, None, None, None, ctypes.byref(rows)),
+        "phj_batch_run": lambda: lib.phj_batch_run(None, 0, None, None, None, None),
+        "phj_table_generate": lambda: lib.phj_table_generate(None, None, ctypes.byref(out)),
+        "phj_table_upload": lambda: lib.phj_table_upload(None, ctypes.byref(desc), ctypes.byref(out)),
+        "phj_output_fingerprint": lambda: lib.phj_output_fingerprint(None, None, keys),
+        "phj_flush_l2": lambda: lib.phj_flush_l2(None),
+        "phj_host_alloc": lambda: lib.phj_host_alloc(None, 16, ctypes.byref(out)),
+    }
+    for name, call in calls.items():
+        assert call() == 1, name  # PHJ_ERR_INVALID_ARGUMENT
