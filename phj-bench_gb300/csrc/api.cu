@@ -1432,8 +1432,8 @@ phj_status phj_ctx_create(int device, phj_ctx ** out)
     phj_ctx * ctx = new (std::nothrow) phj_ctx();
     if (!ctx)
         return PHJ_ERR_OUT_OF_MEMORY;
+    ctx->device = device;
     const phj_status st = guard(ctx, [&] {
-        ctx->device = device;
         PHJ_CUDA(cudaSetDevice(device));
         cudaDeviceProp prop;
         PHJ_CUDA(cudaGetDeviceProperties(&prop, device));
@@ -1470,33 +1470,35 @@ void phj_ctx_destroy(phj_ctx * ctx)
 {
     if (!ctx)
         return;
-    cudaSetDevice(ctx->device);
-    if (ctx->stream)
-        cudaStreamSynchronize(ctx->stream);
-    if (ctx->l2_flush)
-        cudaFree(ctx->l2_flush);
-    if (ctx->d_err)
-        cudaFree(ctx->d_err);
-    if (ctx->host_small)
-        cudaFreeHost(ctx->host_small);
-    for (cudaEvent_t e : ctx->event_pool)
-        cudaEventDestroy(e);
-    for (auto & lv : ctx->live)
-        cudaFreeAsync(lv.first, ctx->stream);
-    if (ctx->stream)
-        cudaStreamSynchronize(ctx->stream);
-    if (ctx->pool)
-        cudaMemPoolDestroy(ctx->pool);
-    if (ctx->stream)
-        cudaStreamDestroy(ctx->stream);
-    if (ctx->h2d)
-        cudaStreamDestroy(ctx->h2d);
-    if (ctx->d2h)
-        cudaStreamDestroy(ctx->d2h);
-    if (ctx->side)
-        cudaStreamDestroy(ctx->side);
-    if (ctx->aux)
-        cudaStreamDestroy(ctx->aux);
+    {
+        DeviceScope dev(ctx);
+        if (ctx->stream)
+            cudaStreamSynchronize(ctx->stream);
+        if (ctx->l2_flush)
+            cudaFree(ctx->l2_flush);
+        if (ctx->d_err)
+            cudaFree(ctx->d_err);
+        if (ctx->host_small)
+            cudaFreeHost(ctx->host_small);
+        for (cudaEvent_t e : ctx->event_pool)
+            cudaEventDestroy(e);
+        for (auto & lv : ctx->live)
+            cudaFreeAsync(lv.first, ctx->stream);
+        if (ctx->stream)
+            cudaStreamSynchronize(ctx->stream);
+        if (ctx->pool)
+            cudaMemPoolDestroy(ctx->pool);
+        if (ctx->stream)
+            cudaStreamDestroy(ctx->stream);
+        if (ctx->h2d)
+            cudaStreamDestroy(ctx->h2d);
+        if (ctx->d2h)
+            cudaStreamDestroy(ctx->d2h);
+        if (ctx->side)
+            cudaStreamDestroy(ctx->side);
+        if (ctx->aux)
+            cudaStreamDestroy(ctx->aux);
+    }
     delete ctx;
 }
 
@@ -1764,6 +1766,7 @@ uint64_t phj_table_gen_distinct(const phj_table * t)
 
 void phj_table_free(phj_ctx * ctx, phj_table * t)
 {
+    DeviceScope dev(ctx);
     if (ctx)
         free_table(ctx, t);
 }
@@ -1931,6 +1934,7 @@ phj_status phj_output_fingerprint(phj_ctx * ctx, const phj_output * out, uint64_
 
 void phj_output_free(phj_ctx * ctx, phj_output * out)
 {
+    DeviceScope dev(ctx);
     if (ctx)
         free_output(ctx, out);
 }

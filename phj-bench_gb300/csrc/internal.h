@@ -341,10 +341,35 @@ void fingerprint(phj_ctx * ctx, const phj_output & out, uint64_t fp[3]);
 void set_partition_smem_limits(int smem_optin);
 void set_build_smem_limits(int smem_optin);
 
-// Runs f, turning exceptions into a status and the context's last error.
+// Makes the context's device current for one call and gives the caller's
+// device back afterwards: a context may be used from any host thread (the
+// request loop's workers are threads of their own) whatever device that
+// thread has current.
+struct DeviceScope
+{
+    int prev = -1;
+    explicit DeviceScope(const phj_ctx * ctx)
+    {
+        int cur = -1;
+        if (ctx && cudaGetDevice(&cur) == cudaSuccess && cur != ctx->device && cudaSetDevice(ctx->device) == cudaSuccess)
+            prev = cur;
+        cudaGetLastError();
+    }
+    ~DeviceScope()
+    {
+        if (prev >= 0)
+            cudaSetDevice(prev);
+    }
+    DeviceScope(const DeviceScope &) = delete;
+    DeviceScope & operator=(const DeviceScope &) = delete;
+};
+
+// Runs f on the context's device, turning exceptions into a status and the
+// context's last error.
 template <class F>
 inline phj_status guard(phj_ctx * ctx, F && f)
 {
+    DeviceScope dev(ctx);
     try
     {
         f();

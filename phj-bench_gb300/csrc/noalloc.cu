@@ -205,6 +205,7 @@ extern "C" phj_status phj_run_chj_noalloc(phj_ctx * ctx, const phj_table * build
         return PHJ_ERR_INVALID_ARGUMENT;
     if (out_rows)
         *out_rows = 0;
+    phjg::DeviceScope dev(ctx);
     try
     {
         phjg::run_chj_noalloc(ctx, *build, *probe, out_capacity, out_keys, out_left, out_right, out_rows);

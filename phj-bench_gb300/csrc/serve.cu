@@ -92,6 +92,7 @@ bool is_small(const phj_server & s, uint64_t id)
 void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
 {
     phj_ctx * ctx = S.slots[slot].ctx;
+    DeviceScope dev(ctx); // this worker thread's CUDA calls go to the slot's device
     const double t_start = S.now_s();
     const size_t n = job.size();
     std::vector<phj_table *> b(n, nullptr), p(n, nullptr);

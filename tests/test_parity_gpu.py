@@ -424,3 +424,37 @@ def test_chj_irregular_blocks_with_packed_payloads(ctx):
             check(b, p, jo, fp)
         finally:
             ctx.set_int("pack_build", 1)
+
+
+def test_contexts_used_from_other_host_threads(ctx):
+    # Every call makes its context's device current for the call: two host
+    # threads, each with its own context, join at the same time and match
+    # the oracle and the same join run on the test's own thread.
+    import threading
+
+    b, p = cases.make("c2_mini")
+    want = run(ctx, "phj-pure", b, p, [4, 4])[1]
+    results, errors = {}, []
+
+    def worker(k):
+        try:
+            c = P.Context(0)
+            try:
+                for scheme in ("phj-pure", "phj", "chj"):
+                    jo, fp, _ = run(c, scheme, b, p, [4, 4])
+                    results[(k, scheme)] = (jo, fp)
+            finally:
+                c.close()
+        except Exception as e:  # reported on the test's thread
+            errors.append(repr(e))
+
+    threads = [threading.Thread(target=worker, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=300)
+    assert not errors, errors
+    assert len(results) == 6
+    for (k, scheme), (jo, fp) in results.items():
+        assert fp == want, (k, scheme)
+    check(b, p, results[(0, "phj")][0], want)
