@@ -13,8 +13,11 @@
  * reference's C++ signatures on top of it.
  *
  * Threading: a context is used by one host thread at a time (the reference's
- * run* functions are likewise blocking calls from one thread).  Every run
- * call is blocking: it returns when the join is complete on the device.
+ * run* functions are likewise blocking calls from one thread); which thread
+ * does not matter, and contexts on different threads run concurrently.  Each
+ * call makes the context's device current for its duration and gives the
+ * caller's current device back on return.  Every run call is blocking: it
+ * returns when the join is complete on the device.
  */
 #ifndef PHJ_GPU_H
 #define PHJ_GPU_H
