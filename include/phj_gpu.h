@@ -174,7 +174,10 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's
  *        batches take the configuration's first pass;
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
- *        leaf BUILDING before the probe, so its waits run out. */
+ *        leaf BUILDING before the probe, so its waits run out;
+ *   "test_fail_build": test hook, 0 (default) off; 1 makes the host-buffer
+ *        joins return PHJ_ERR_CUDA right after the build shuffle, with
+ *        their uploads still queued. */
 phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);
 /* Reads an option above, or a device property: "device", "num_sms",
  * "l2_bytes", "wait_limit_ms". */

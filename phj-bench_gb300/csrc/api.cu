@@ -927,6 +927,22 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     *out = o;
 }
 
+// On every exit from a host-buffer join, errors included, waits for the
+// copies still queued on the h2d and d2h streams, so that no buffer the
+// table guard or the scratch hands back to the pool (both free in the
+// compute stream's order only) is still read or written by a copy.
+struct CopyDrain
+{
+    phj_ctx * c;
+    ~CopyDrain()
+    {
+        if (c->h2d)
+            cudaStreamSynchronize(c->h2d);
+        if (c->d2h)
+            cudaStreamSynchronize(c->d2h);
+    }
+};
+
 // PHJ-PURE with the inputs and the output in host memory.  The build side
 // is uploaded whole; the probe side streams through in chunks on three
 // streams: chunk c+1 uploads (h2d) while chunk c is partitioned by the first
@@ -963,6 +979,7 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     // device buffers, all allocated on the compute stream before any copy
     phj_table * B = alloc_table(ctx, hb.schema, B_rows);
     std::unique_ptr<phj_table, std::function<void(phj_table *)>> B_guard(B, [ctx](phj_table * t) { free_table(ctx, t); });
+    const CopyDrain drain{ctx}; // destroyed before B_guard and the scratch
     Cols in[2];
     for (auto & c : in)
         c = alloc_cols_like(s, hp.schema, C);
@@ -1006,6 +1023,8 @@ static void run_phj_pure_host(phj_ctx * ctx, const phj_block_stream & hb, const 
     // -------- BUILD SHUFFLE + BUILD (src/PHJ.cpp:220-282) --------
     PHJ_CUDA(cudaStreamWaitEvent(S, build_up, 0));
     radix_partition(ctx, s, bin, B_rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    if (ctx->test_fail_build)
+        throw Error(PHJ_ERR_CUDA, "test_fail_build: failure injected after the build shuffle");
     PHJ_CUDA(cudaEventRecord(ev[1], S));
     LeafTables lt;
     lt.next = s.get<uint64_t>(B_rows);
@@ -1184,6 +1203,7 @@ static void run_phj_bep_host(phj_ctx * ctx, const phj_block_stream & hb, const p
     // device buffers, all allocated on the compute stream before any copy
     phj_table * B = alloc_table(ctx, hb.schema, B_rows);
     std::unique_ptr<phj_table, std::function<void(phj_table *)>> B_guard(B, [ctx](phj_table * t) { free_table(ctx, t); });
+    const CopyDrain drain{ctx}; // destroyed before B_guard and the scratch
     Cols in[2];
     for (auto & c : in)
         c = alloc_cols_like(s, hp.schema, C);
@@ -1238,6 +1258,8 @@ static void run_phj_bep_host(phj_ctx * ctx, const phj_block_stream & hb, const p
     // first use (src/PHJBep.cpp:128-141) --------
     PHJ_CUDA(cudaStreamWaitEvent(S, build_up, 0));
     radix_partition(ctx, s, bin, B_rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    if (ctx->test_fail_build)
+        throw Error(PHJ_ERR_CUDA, "test_fail_build: failure injected after the build shuffle");
     PHJ_CUDA(cudaEventRecord(ev[1], S));
     LeafTables lt;
     lt.next = s.get<uint64_t>(B_rows);
@@ -1536,6 +1558,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
+    else if (std::strcmp(name, "test_fail_build") == 0 && (value == 0 || value == 1))
+        ctx->test_fail_build = (int)value;
     else
         return PHJ_ERR_INVALID_ARGUMENT;
     return PHJ_OK;
@@ -1565,6 +1589,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
+    else if (std::strcmp(name, "test_fail_build") == 0)
+        *value = ctx->test_fail_build;
     else if (std::strcmp(name, "device") == 0)
         *value = ctx->device;
     else if (std::strcmp(name, "num_sms") == 0)

@@ -34,7 +34,7 @@ STATUS = {
     0: "PHJ_OK", 1: "PHJ_ERR_INVALID_ARGUMENT", 2: "PHJ_ERR_CUDA", 3: "PHJ_ERR_OUT_OF_MEMORY",
     4: "PHJ_ERR_UNSUPPORTED", 5: "PHJ_ERR_DEVICE_TIMEOUT", 6: "PHJ_ERR_NO_DEVICE", 7: "PHJ_ERR_CAPACITY",
 }
-ERR_INVALID_ARGUMENT, ERR_DEVICE_TIMEOUT = 1, 5
+ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_DEVICE_TIMEOUT = 1, 2, 5
 
 
 class PhjError(RuntimeError):

@@ -458,3 +458,36 @@ def test_contexts_used_from_other_host_threads(ctx):
     for (k, scheme), (jo, fp) in results.items():
         assert fp == want, (k, scheme)
     check(b, p, results[(0, "phj")][0], want)
+
+
+@pytest.mark.parametrize("scheme", ["phj-pure", "phj"])
+def test_host_buffer_failure_after_build_shuffle_leaves_context_usable(ctx, scheme):
+    # A host-side failure while the probe chunks' uploads are still queued:
+    # the call returns the error after draining its copy streams, and the
+    # next host-buffer join on the same context (reusing the pooled memory
+    # those copies wrote) is bit-exact.
+    b, p = cases.make("c2_mini")
+    expected = O.join_rows(b, p)
+    keys, left, right = host_out(ctx, b, p, len(expected))
+
+    def join():
+        if scheme == "phj":
+            return ctx.run_phj_bep_host(b, p, [4, 4], 1, keys, left, right)[0]
+        return ctx.run_phj_pure_host(b, p, [4, 4], keys, left, right)[0]
+
+    ctx.set_int("host_chunk_rows", 8192)
+    try:
+        for _ in range(2):
+            ctx.set_int("test_fail_build", 1)
+            try:
+                with pytest.raises(P.PhjError) as e:
+                    join()
+                assert e.value.status == P.ERR_CUDA and "test_fail_build" in str(e.value)
+            finally:
+                ctx.set_int("test_fail_build", 0)
+            rows = join()
+            assert rows == len(expected)
+            jo = P.JoinOutput(b.types, p.types, keys[:rows], [c[:rows] for c in left], [c[:rows] for c in right])
+            assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
+    finally:
+        ctx.set_int("host_chunk_rows", 16 << 20)
