@@ -615,7 +615,7 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
     uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
     LeafTables lt;
-    bool grouped = false, packing = false;
+    bool grouped = false;
     try
     {
         radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
@@ -642,7 +642,6 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
         }
         PHJ_CUDA(cudaEventRecord(ev[8], ctx->stream));
         ctx->stream = main_stream;
-        packing = true;
 
         // -------- BUILD: per-leaf tables (src/PHJ.cpp:260-282) --------
         lt.next = s.get<uint64_t>(B.rows);
@@ -656,9 +655,10 @@ static void run_phj_pure(phj_ctx * ctx, const phj_table & B, const phj_table & P
     }
     catch (...)
     {
+        // the side and aux streams' buffers are freed with the scratch
         if (mat)
-            cudaStreamSynchronize(ctx->side); // its buffers are freed with the scratch
-        if (packing)
+            cudaStreamSynchronize(ctx->side);
+        if (ctx->aux)
             cudaStreamSynchronize(ctx->aux);
         throw;
     }
