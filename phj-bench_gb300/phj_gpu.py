@@ -217,12 +217,21 @@ class BlockStream:
 
     def __post_init__(self):
         self.keys = np.ascontiguousarray(self.keys, dtype=np.uint64)
+        if self.keys.ndim != 1:
+            raise PhjError(ERR_INVALID_ARGUMENT, "the key column must be one-dimensional")
+        if len(self.payloads) != len(self.types) or len(self.types) > MAX_PAYLOADS:
+            raise PhjError(ERR_INVALID_ARGUMENT, f"{len(self.payloads)} payload columns for {len(self.types)} types")
         self.payloads = [column_view(p, t) for p, t in zip(self.payloads, self.types)]
+        n = len(self.keys)
+        for i, p in enumerate(self.payloads):
+            if len(p) != n:
+                raise PhjError(ERR_INVALID_ARGUMENT, f"payload column {i} has {len(p)} rows, the keys {n}")
         if self.block_rows is None:
-            n = len(self.keys)
             full, rem = divmod(n, PIPELINE_BLOCK_ROWS)
             self.block_rows = np.array([PIPELINE_BLOCK_ROWS] * full + ([rem] if rem else []), dtype=np.uint32)
         self.block_rows = np.ascontiguousarray(self.block_rows, dtype=np.uint32)
+        if int(self.block_rows.sum(dtype=np.uint64)) != n:
+            raise PhjError(ERR_INVALID_ARGUMENT, "block_rows do not add up to the rows of the stream")
 
     @property
     def total_rows(self) -> int:
@@ -402,14 +411,36 @@ class Context:
         d.location = 0
         return d
 
+    @staticmethod
+    def _host_out(build: BlockStream, probe: BlockStream, out_keys: np.ndarray, out_left: Sequence[np.ndarray],
+                  out_right: Sequence[np.ndarray]):
+        """Column pointers of caller-owned host output columns, checked
+        against the two schemas: the library writes up to len(out_keys) rows
+        into every column, so each must be contiguous, of its type and at
+        least that long."""
+        def check(a, dtype, what, cols=None):
+            if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+                raise PhjError(ERR_INVALID_ARGUMENT, f"{what}: a C-contiguous {np.dtype(dtype).name} array is required")
+            if (a.ndim, a.shape[1:]) != ((2, (cols,)) if cols else (1, ())) or len(a) < len(out_keys):
+                raise PhjError(ERR_INVALID_ARGUMENT, f"{what}: shape {a.shape} cannot hold {len(out_keys)} rows")
+
+        check(out_keys, np.uint64, "output keys")
+        ptrs = []
+        for side, types, cols in (("left", build.types, out_left), ("right", probe.types, out_right)):
+            if len(cols) != len(types):
+                raise PhjError(ERR_INVALID_ARGUMENT, f"{len(cols)} {side} output columns for {len(types)} payload types")
+            for i, (c, t) in enumerate(zip(cols, types)):
+                check(c, np.uint64 if t == U128 else TYPE_DTYPE[t], f"{side} output column {i}", 2 if t == U128 else None)
+            ptrs.append((C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in cols]))
+        return ptrs
+
     def run_phj_pure_host(self, build: BlockStream, probe: BlockStream, pass_bits: Sequence[int], out_keys: np.ndarray,
                           out_left: Sequence[np.ndarray], out_right: Sequence[np.ndarray]):
         """phj_run_phj_pure_host: host inputs, host output columns (pinned
         for full speed).  Returns (output rows, PhjResultC)."""
         db, dp = self._desc(build), self._desc(probe)
         bits = (C.c_uint8 * max(1, len(pass_bits)))(*pass_bits)
-        lp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_left])
-        rp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_right])
+        lp, rp = self._host_out(build, probe, out_keys, out_left, out_right)
         rows = C.c_uint64()
         r = PhjResultC()
         self._check(self.lib.phj_run_phj_pure_host(self.ptr, C.byref(db), C.byref(dp), bits, len(pass_bits), len(out_keys),
@@ -422,8 +453,7 @@ class Context:
         for full speed).  Returns (output rows, BepResultC)."""
         db, dp = self._desc(build), self._desc(probe)
         bits = (C.c_uint8 * max(1, len(pass_bits)))(*pass_bits)
-        lp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_left])
-        rp = (C.c_void_p * MAX_PAYLOADS)(*[c.ctypes.data for c in out_right])
+        lp, rp = self._host_out(build, probe, out_keys, out_left, out_right)
         rows = C.c_uint64()
         r = BepResultC()
         self._check(self.lib.phj_run_phj_bep_host(self.ptr, C.byref(db), C.byref(dp), bits, len(pass_bits), budget_mib, len(out_keys),
