@@ -349,7 +349,11 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
     const uint32_t nb = 1u << g.b, mask = nb - 1;
     uint32_t * bins = reinterpret_cast<uint32_t *>(dsort + kT);
     uint32_t * excl = bins + nb;
-    uint32_t * cursor = excl + nb;
+    // running output cursors per digit, two arrays in turn: the scan of tile
+    // t writes tile t+1's cursors while tile t's are still being read, so no
+    // barrier is needed to advance them
+    uint32_t * cur = excl + nb;
+    uint32_t * nxt = cur + nb;
 
     const uint64_t n_tiles = ceil_div(g.n, kT);
     const uint64_t t_begin = (uint64_t)blockIdx.x * g.tiles_per_cta;
@@ -358,7 +362,7 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
         return;
     for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
     {
-        cursor[d] = offs[(uint64_t)d * gridDim.x + blockIdx.x];
+        cur[d] = offs[(uint64_t)d * gridDim.x + blockIdx.x];
         bins[d] = 0;
     }
     if (threadIdx.x == 0)
@@ -428,7 +432,7 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
         const uint32_t nbi = (bi + stages - 1) % stages;
         if (threadIdx.x == 0 && t + stages - 1 < t_end && tma_ok(t + stages - 1))
             issue(t + stages - 1, nbi);
-        // (bins were zeroed with the cursor update that ended the last tile)
+        // (bins were zeroed by the last tile's scan)
 
         const uint64_t * bk = reinterpret_cast<const uint64_t *>(buf);
         uint32_t dg[RPT], rk[RPT];
@@ -445,8 +449,9 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
             }
         }
         __syncthreads();
-        // exclusive scan of the digit counts by the first warp alone: one
-        // barrier instead of the block scan's three
+        // exclusive scan of the digit counts by the first warp alone (one
+        // barrier instead of the block scan's three), which also advances
+        // the cursors for the next tile and zeroes the counts
         if (threadIdx.x < 32)
         {
             const uint32_t lane = threadIdx.x;
@@ -468,8 +473,11 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
             for (uint32_t i = 0; i < per; ++i)
                 if (b0 + i < nb)
                 {
+                    const uint32_t c = bins[b0 + i];
                     excl[b0 + i] = run;
-                    run += bins[b0 + i];
+                    run += c;
+                    nxt[b0 + i] = cur[b0 + i] + c;
+                    bins[b0 + i] = 0;
                 }
         }
         __syncthreads();
@@ -493,7 +501,7 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
             {
                 const uint32_t d = dsort[pos];
                 src[j] = inv[pos];
-                dest[j] = cursor[d] + (pos - excl[d]);
+                dest[j] = cur[d] + (pos - excl[d]);
             }
         }
         p1_write_column<uint64_t, RPT>(buf, out.keys, src, dest, cnt);
@@ -509,12 +517,13 @@ __global__ void __launch_bounds__(kP1NT, kMinB) k_p1_scatter(const __grid_consta
                 default: p1_write_column<uint4, RPT>(cb, (uint4 *)out.col[c], src, dest, cnt); break;
             }
         }
-        __syncthreads(); // cursor/bins reuse; this buffer is refilled next iteration
-        for (uint32_t d = threadIdx.x; d < nb; d += kP1NT)
-        {
-            cursor[d] += bins[d];
-            bins[d] = 0; // for the next tile's ranks
-        }
+        // No barrier here: the next tile's first barrier (after its wait)
+        // comes before this buffer is refilled, before the counts are
+        // ranked into again and before `cur` is overwritten as the next
+        // tile's `nxt`.
+        uint32_t * t_swap = cur;
+        cur = nxt;
+        nxt = t_swap;
     }
     // Bulk copies still in flight (only after a timeout) must land before
     // the CTA's shared memory is released.
@@ -596,7 +605,7 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
             for (uint32_t c = 0; c < src.n; ++c)
                 buf += kT * src.width[c];
             buf = (buf + 127) & ~127ull;
-            const uint64_t need_rs = st * buf + 4 * kT + 3ull * nb * 4;
+            const uint64_t need_rs = st * buf + 4 * kT + 4ull * nb * 4;
             if (need_rs + 2048 > ctx->smem_optin)
                 continue;
             const uint64_t inflight = (st - 1) * buf;
@@ -617,7 +626,7 @@ static void first_pass(phj_ctx * ctx, Scratch & s, const Cols & src, const Cols 
         off += kT * src.width[c];
     }
     sm.buf_bytes = (off + 127) & ~127u;
-    const size_t need = (size_t)stages * sm.buf_bytes + 4ull * kT + 3ull * nb * 4;
+    const size_t need = (size_t)stages * sm.buf_bytes + 4ull * kT + 4ull * nb * 4;
     int per_sm = 1;
     auto kern = ctx->p1_beside ? (rpt == 8 ? k_p1_scatter<8, 2> : rpt == 4 ? k_p1_scatter<4, 2> : k_p1_scatter<2, 2>)
                                : (rpt == 8 ? k_p1_scatter<8, 1> : rpt == 4 ? k_p1_scatter<4, 1> : k_p1_scatter<2, 1>);
