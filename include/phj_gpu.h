@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHJ_GPU_ABI_VERSION 1u
+#define PHJ_GPU_ABI_VERSION 2u
 #define PHJ_MAX_PAYLOADS 8u /* payload columns per side */
 
 /* Error codes.  The reference throws std::invalid_argument / std::bad_alloc
@@ -379,13 +379,17 @@ void phj_output_free(phj_ctx *ctx, phj_output *out);
 
 /* ---- measurement hooks ------------------------------------------------------ */
 
-/* Per-kernel device times of the last run (CUDA events on the context's
- * stream).  Fills up to `cap` entries; returns the number recorded. */
+/* Per-kernel device times of the last run (CUDA events on the stream each
+ * kernel was launched on).  Fills up to `cap` entries; returns the number
+ * recorded.  `start_ms` places each launch on the run's timeline (0 = the
+ * earliest timed launch), so a caller can tell which launches overlapped
+ * launches on another of the context's streams. */
 typedef struct phj_kernel_time {
     char name[32];
     double ms;
     uint64_t rows;   /* rows the launch processed */
     uint64_t bytes;  /* algorithmic bytes the launch read+wrote */
+    double start_ms; /* start of the launch after the run's earliest timed launch */
 } phj_kernel_time;
 uint32_t phj_last_kernel_times(const phj_ctx *ctx, phj_kernel_time *out, uint32_t cap);
 /* Number of this library's kernel launches issued since the context was

@@ -1970,6 +1970,9 @@ uint32_t phj_last_kernel_times(const phj_ctx * ctx, phj_kernel_time * out, uint3
     if (!ctx || !out)
         return 0;
     uint32_t n = 0;
+    // start offsets from the first record, then shifted so the earliest
+    // launch (possibly on another stream) is at 0
+    double first = 0.0;
     for (const auto & r : ctx->records)
     {
         if (n >= cap)
@@ -1977,16 +1980,25 @@ uint32_t phj_last_kernel_times(const phj_ctx * ctx, phj_kernel_time * out, uint3
         phj_kernel_time & k = out[n++];
         std::memset(&k, 0, sizeof(k));
         std::strncpy(k.name, r.name.c_str(), sizeof(k.name) - 1);
-        float ms = 0.f;
+        float ms = 0.f, at = 0.f;
         if (cudaEventElapsedTime(&ms, r.start, r.stop) != cudaSuccess)
         {
             cudaGetLastError();
             ms = -1.f;
         }
+        if (cudaEventElapsedTime(&at, ctx->records.front().start, r.start) != cudaSuccess)
+        {
+            cudaGetLastError();
+            at = 0.f;
+        }
         k.ms = ms;
         k.rows = r.rows;
         k.bytes = r.bytes;
+        k.start_ms = at;
+        first = std::min(first, (double)at);
     }
+    for (uint32_t i = 0; i < n; ++i)
+        out[i].start_ms -= first;
     return n;
 }
 

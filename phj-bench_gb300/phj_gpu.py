@@ -22,6 +22,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("PHJ_GPU_LIB") or os.path.join(HERE, "libphj_gpu.so")
 MAX_PAYLOADS = 8
+ABI_VERSION = 2  # PHJ_GPU_ABI_VERSION of include/phj_gpu.h these structures follow
 
 # PayloadType codes, src/Types.h:23-30
 U8, U16, U32, U64, U128 = 0, 1, 2, 3, 4
@@ -85,7 +86,7 @@ class GenSpec(C.Structure):
 
 
 class KernelTime(C.Structure):
-    _fields_ = [("name", C.c_char * 32), ("ms", C.c_double), ("rows", C.c_uint64), ("bytes", C.c_uint64)]
+    _fields_ = [("name", C.c_char * 32), ("ms", C.c_double), ("rows", C.c_uint64), ("bytes", C.c_uint64), ("start_ms", C.c_double)]
 
 
 class BatchResultC(C.Structure):
@@ -176,6 +177,8 @@ def load() -> C.CDLL:
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
+    if lib.phj_abi_version() != ABI_VERSION:
+        raise ImportError(f"{LIB_PATH} has ABI version {lib.phj_abi_version()}, these bindings need {ABI_VERSION}: rebuild it")
     _lib = lib
     return lib
 
@@ -536,7 +539,8 @@ class Context:
     def kernel_times(self) -> List[dict]:
         arr = (KernelTime * 256)()
         n = self.lib.phj_last_kernel_times(self.ptr, arr, 256)
-        return [{"name": arr[i].name.decode(), "ms": arr[i].ms, "rows": arr[i].rows, "bytes": arr[i].bytes} for i in range(n)]
+        return [{"name": arr[i].name.decode(), "ms": arr[i].ms, "rows": arr[i].rows, "bytes": arr[i].bytes, "start_ms": arr[i].start_ms}
+                for i in range(n)]
 
     def launch_count(self) -> int:
         return self.lib.phj_launch_count(self.ptr)

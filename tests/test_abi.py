@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.phj_abi_version() == 1
+    assert lib.phj_abi_version() == P.ABI_VERSION == 2
 
 
 @pytest.mark.parametrize("parts,passes,want", [
