@@ -225,12 +225,14 @@ def measured_peak():
         return 6800.0, "fallback 6.8 TB/s (MEASURED_PEAKS.json absent)"
 
 
-def profiled_traffic(kernel, workload):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+def profiled_traffic(kernel, workload, scale=1.0):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary: a
+    full-size launch, scaled by the rows a `--scale`d run processes (the
+    figures grow in proportion to the rows)."""
     try:
         d = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
         e = d.get(workload, {}).get(kernel)
-        return e["dram_bytes_per_launch"] if e else None
+        return int(e["dram_bytes_per_launch"] * scale) if e else None
     except Exception:
         return None
 
@@ -466,7 +468,7 @@ def main():
                    "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set,
                    "autotuned": tuned},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload),
+                     "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload, args.scale),
                      "bytes_per_launch": bytes_per_launch, "ms_per_launch": avg_ms, "launches_timed": dom["launches"],
                      "selection": "largest time in launches that overlapped no other launch", "peak_source": peak_src},
         "join_roofline": {"bytes_min": bmin, "achieved_gbs": join_gbs, "frac": join_gbs / peak,
