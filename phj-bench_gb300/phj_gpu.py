@@ -376,9 +376,15 @@ class Context:
         if st != 0:
             raise PhjError(st, "phj_ctx_create failed (is a GB300 visible?)")
         self.ptr = p
+        self._pinned = []  # phj_host_alloc blocks of pinned(), freed by close()
 
     def close(self):
+        """Destroys the context and frees the pinned host memory that
+        pinned() handed out (arrays over it must not be used afterwards)."""
         if self.ptr:
+            for h in self._pinned:
+                self.lib.phj_host_free(self.ptr, h)
+            self._pinned = []
             self.lib.phj_ctx_destroy(self.ptr)
             self.ptr = None
 
@@ -553,6 +559,7 @@ class Context:
         nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
         p = C.c_void_p()
         self._check(self.lib.phj_host_alloc(self.ptr, nbytes, C.byref(p)))
+        self._pinned.append(p.value)
         buf = (C.c_uint8 * max(nbytes, 1)).from_address(p.value)
         arr = np.frombuffer(buf, dtype=np.uint8, count=nbytes).view(dtype).reshape(shape)
         return arr

@@ -46,3 +46,36 @@ def test_schemes_agree_at_full_size(ctx, wl, bits, unique):
             assert rows > p.rows // 2  # half of the probe keys match, ~4 build rows each
     finally:
         b.free(), p.free()
+
+
+@pytest.mark.parametrize("scheme", ["phj-pure", "phj"])
+def test_host_buffer_join_at_full_size_matches_device_join(ctx, scheme):
+    # 16M x 256M through the host-buffer entry points (upload, join and
+    # download overlapped in chunks or budget-sized batches): the rows that
+    # land in host memory have the device join's fingerprint.
+    import numpy as np
+
+    import oracle as O
+    import phj_gpu as P
+
+    c = P.Context(0)  # its own context: the pinned output columns go with it
+    try:
+        b, p = bench.make_tables(c, "c2")
+        try:
+            budget = bench.BEP_BUDGET_PER_GROUP.get("c4", 32) * c.get_int("num_sms")
+            want = fingerprint(c, scheme, b, p, [8, 8], budget)
+            hb, hp = b.download(), p.download()
+        finally:
+            b.free(), p.free()
+        cap = want[0]
+        keys = c.pinned((cap,), np.uint64)
+        left = [c.pinned((cap,), P.TYPE_DTYPE[t]) for t in hb.types]
+        right = [c.pinned((cap,), P.TYPE_DTYPE[t]) for t in hp.types]
+        if scheme == "phj":
+            rows, _ = c.run_phj_bep_host(hb, hp, [8, 8], budget, keys, left, right)
+        else:
+            rows, _ = c.run_phj_pure_host(hb, hp, [8, 8], keys, left, right)
+        assert rows == cap
+        assert O.columns_fingerprint(P.JoinOutput(hb.types, hp.types, keys, left, right)) == want
+    finally:
+        c.close()
