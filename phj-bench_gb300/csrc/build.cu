@@ -346,12 +346,17 @@ void build_leaf_tables(phj_ctx * ctx, Scratch & s, const Cols & build_part, cons
         lt.any_dup = 1; // unknown until the tables are built: chains are followed
         return;
     }
-    const uint32_t smem_cells = (uint32_t)std::min<uint64_t>(max_cap, kSmemCellsMax);
+    // Tables are built in shared memory and copied out when two CTAs fit
+    // on an SM; larger ones (one resident CTA per SM would leave the SMs
+    // idling through each leaf's copy-out) are built in place, in global
+    // memory that stays in L2 (1M x 8M, 256 leaves of 8192 cells: 0.310 ->
+    // 0.304 ms a join).
+    const uint32_t smem_cells =
+        max_cap * sizeof(Cell) * 2 <= ctx->smem_optin ? (uint32_t)std::min<uint64_t>(max_cap, kSmemCellsMax) : 0u;
     int * any_dup = reinterpret_cast<int *>(small + 1);
     {
         KTimer kt(ctx, "build_leaf_tables", 0, 0);
-        // leaves of more than 1024 rows (few, large leaves: one resident CTA
-        // per SM by shared memory) get 1024 threads
+        // leaves of more than 1024 rows get 1024 threads
         auto kb = lt.max_rows > 1024 ? k_build_leaf<1024> : k_build_leaf<kBuildNT>;
         kb<<<n_leaves, lt.max_rows > 1024 ? 1024 : kBuildNT, (size_t)smem_cells * sizeof(Cell), ctx->stream>>>(build_part.keys, leaf_off, table_off, lt.uniform_log2cap,
                                                                                             smem_cells, lt.cells, lt.next, lt.meta, any_dup);
