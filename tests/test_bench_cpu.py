@@ -14,3 +14,10 @@ def test_launch_overlaps():
     assert [bench.launch_overlaps(run, i) for i in range(4)] == [True, True, False, False]
     # back-to-back launches of one stream touch but do not overlap
     assert not bench.launch_overlaps([rec("a", 0.0, 1.0), rec("b", 1.0, 1.0)], 0)
+
+
+def test_profiled_traffic_scales_with_rows():
+    full = bench.profiled_traffic("probe_project", "c2")
+    assert full and full > 10e9  # a full-size launch moves about 12 GB
+    assert bench.profiled_traffic("probe_project", "c2", 0.125) == int(full * 0.125)
+    assert bench.profiled_traffic("no_such_kernel", "c2") is None
