@@ -88,13 +88,17 @@ __device__ __forceinline__ uint32_t chain_len(const uint64_t * __restrict__ next
 }
 
 // A warp per chunk of 256 probe rows: heads, and the chunk's output rows.
+// The batch's output rows are also summed in 64 bits (one atomic per warp),
+// so the host can refuse a batch whose 32-bit chunk offsets would wrap.
 __global__ void __launch_bounds__(kBNT) k_batch_lookup(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ chunks,
                                                        const Cell * __restrict__ cells, const uint64_t * __restrict__ next,
-                                                       uint32_t * __restrict__ heads, uint32_t * __restrict__ counts)
+                                                       uint32_t * __restrict__ heads, uint32_t * __restrict__ counts,
+                                                       unsigned long long * __restrict__ out_rows64)
 {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_chunks = chunks[n];
     const uint64_t warps = ((uint64_t)gridDim.x * kBNT) >> 5;
+    unsigned long long warp_rows = 0;
     for (uint64_t c = ((uint64_t)blockIdx.x * kBNT + threadIdx.x) >> 5; c < n_chunks; c += warps)
     {
         const uint32_t j = find_join(chunks, n, c);
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(kBNT) k_batch_lookup(const BatchJoin * __restr
         const uint64_t cap = 1ull << J.log2cap;
         const Cell * tab = cells + J.cell_off;
         const uint64_t row0 = (c - chunks[j]) * kBChunk + lane;
-        uint32_t total = 0;
+        unsigned long long total = 0;
 #pragma unroll 4
         for (int k = 0; k < kBRPT; ++k)
         {
@@ -123,8 +127,11 @@ __global__ void __launch_bounds__(kBNT) k_batch_lookup(const BatchJoin * __restr
         for (int o = 16; o > 0; o >>= 1)
             total += __shfl_xor_sync(0xffffffffu, total, o);
         if (lane == 0)
-            counts[c] = total;
+            counts[c] = (uint32_t)min(total, 0xFFFFFFFFull); // the host refuses the batch above 2^32 - 1 rows
+        warp_rows += total;
     }
+    if (lane == 0 && warp_rows)
+        atomicAdd(out_rows64, warp_rows);
 }
 
 __global__ void k_batch_totals(const uint64_t * __restrict__ chunks, const uint32_t * __restrict__ offs, uint32_t n, uint64_t * __restrict__ totals)
@@ -246,6 +253,8 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
     uint64_t * d_tiles = s.get<uint64_t>(n + 1);
     uint64_t * d_chunks = s.get<uint64_t>(n + 1);
     uint64_t * d_totals = s.get<uint64_t>(std::max<uint32_t>(n, 1));
+    unsigned long long * d_rows64 = s.get<unsigned long long>(1);
+    PHJ_CUDA(cudaMemsetAsync(d_rows64, 0, sizeof(unsigned long long), ctx->stream));
     BatchJoin * d_desc = s.get<BatchJoin>(std::max<uint32_t>(n, 1));
     PHJ_CUDA(cudaMemcpyAsync(d_tiles, tiles.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
     PHJ_CUDA(cudaMemcpyAsync(d_chunks, chunks.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
@@ -268,14 +277,19 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
         {
             KTimer kt(ctx, "batch_lookup", prows, prows * (8 + 4));
             k_batch_lookup<<<grid_for(ctx, ceil_div(chunks[n], kBNT / 32)), kBNT, 0, ctx->stream>>>(d_desc, n, d_chunks, d_cells, d_next, d_heads,
-                                                                                                     d_counts);
+                                                                                                     d_counts, d_rows64);
             PHJ_LAUNCHED(ctx, "batch_lookup");
         }
         scan_u32(ctx, s, d_counts, d_counts, chunks[n]);
         k_batch_totals<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(d_chunks, d_counts, n, d_totals);
         PHJ_LAUNCHED(ctx, "batch_totals");
+        unsigned long long rows64 = 0;
         PHJ_CUDA(cudaMemcpyAsync(totals.data(), d_totals, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
+        PHJ_CUDA(cudaMemcpyAsync(&rows64, d_rows64, sizeof(rows64), cudaMemcpyDeviceToHost, ctx->stream));
         PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (rows64 >= (1ull << 32))
+            throw Error(PHJ_ERR_CAPACITY, "the batch has " + std::to_string(rows64) +
+                                              " output rows; batched joins place at most 2^32 - 1 in all (run large joins on their own)");
     }
     std::vector<phj_output *> made(n, nullptr);
     try
