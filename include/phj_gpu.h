@@ -287,7 +287,9 @@ phj_status phj_run_phj_bep_host(phj_ctx *ctx, const phj_block_stream *build, con
  * scan, project, each over all n joins through a device work list of
  * (join, tile) items); outs[j] receives join j's output, the same multiset
  * of rows as a single-join entry point gives for that pair.  Meant for small
- * and medium joins, whose single launches would not fill the device. */
+ * and medium joins, whose single launches would not fill the device; a
+ * batch whose joins have 2^32 output rows or more in all returns
+ * PHJ_ERR_CAPACITY (run large joins on their own). */
 phj_status phj_batch_run(phj_ctx *ctx, uint32_t n, const phj_table *const *builds, const phj_table *const *probes,
                          phj_output **outs, phj_batch_result *result);
 
