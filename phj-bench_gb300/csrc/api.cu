@@ -1969,6 +1969,7 @@ uint32_t phj_last_kernel_times(const phj_ctx * ctx, phj_kernel_time * out, uint3
 {
     if (!ctx || !out)
         return 0;
+    DeviceScope dev(ctx);
     uint32_t n = 0;
     // start offsets from the first record, then shifted so the earliest
     // launch (possibly on another stream) is at 0
