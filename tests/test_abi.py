@@ -130,3 +130,12 @@ def test_entry_points_reject_a_null_context_without_a_device(lib):
     }
     for name, call in calls.items():
         assert call() == 1, name  # PHJ_ERR_INVALID_ARGUMENT
+
+
+@pytest.mark.parametrize("cmd", [["gcc", "-std=c99", "-x", "c"], ["g++", "-std=c++17", "-x", "c++"]])
+def test_header_is_plain_c_and_cpp(cmd):
+    # FFI users (ctypes, cgo, JNI shims) bind the header from C
+    import subprocess
+    r = subprocess.run(cmd + ["-Wall", "-Wextra", "-Werror", "-fsyntax-only", os.path.join(ROOT, "include", "phj_gpu.h")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
