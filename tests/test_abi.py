@@ -139,3 +139,15 @@ def test_header_is_plain_c_and_cpp(cmd):
     r = subprocess.run(cmd + ["-Wall", "-Wextra", "-Werror", "-fsyntax-only", os.path.join(ROOT, "include", "phj_gpu.h")],
                        capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_plain_c_caller_links_and_calls_the_library(lib, tmp_path):
+    import subprocess
+    so_dir = os.path.dirname(P.LIB_PATH)
+    exe = str(tmp_path / "c_abi_main")
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "c_abi_main.c"), "-L", so_dir, "-lphj_gpu", f"-Wl,-rpath,{so_dir}", "-o", exe],
+                   check=True)
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
+    assert out[:7] == ["abi", "2", "radix", "0", "2", "8", "8"]
+    assert out[7] == "ctx" and int(out[8]) in (0, 6)  # PHJ_OK on a GPU machine, PHJ_ERR_NO_DEVICE without one
