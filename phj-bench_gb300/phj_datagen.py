@@ -84,8 +84,9 @@ class Perm:
         return y
 
 
-def payload_columns(seed: int, types: Sequence[int], rows: int) -> List[np.ndarray]:
-    idx = np.arange(rows, dtype=np.uint64)
+def payload_columns(seed: int, types: Sequence[int], rows: int, start: int = 0) -> List[np.ndarray]:
+    """Payload columns of rows [start, start + rows)."""
+    idx = np.arange(start, start + rows, dtype=np.uint64)
     cols = []
     for c, t in enumerate(types):
         lo = rand64(seed, 16 + c, idx)
@@ -97,13 +98,15 @@ def payload_columns(seed: int, types: Sequence[int], rows: int) -> List[np.ndarr
     return cols
 
 
-def gen_keys(kind: int, rows: int, seed: int, key_seed: int, domain: int = 0, match_permille: int = 1000):
-    """Keys of generator kinds 0, 1, 3, 4 (see include/phj_gpu.h, phj_gen_spec)."""
-    idx = np.arange(rows, dtype=np.uint64)
+def gen_keys(kind: int, rows: int, seed: int, key_seed: int, domain: int = 0, match_permille: int = 1000, start: int = 0,
+             total: int = 0):
+    """Keys of generator kinds 0, 1, 3, 4 (see include/phj_gpu.h, phj_gen_spec)
+    for rows [start, start + rows) of a side of `total` rows (default: rows)."""
+    idx = np.arange(start, start + rows, dtype=np.uint64)
     if kind == 0:
         return key_of(key_seed, idx)
     if kind == 1:
-        return Perm(rows, seed)(idx) + np.uint64(1)
+        return Perm(total or rows, seed)(idx) + np.uint64(1)
     if kind == 3:
         return uniform_below(rand64(seed, 1, idx), domain) + np.uint64(1)
     if kind == 4:
@@ -152,14 +155,15 @@ def _zh_integral_inv(s, x):
     return np.exp(h1 * x)
 
 
-def zipf_ranks(n: int, theta: float, seed: int, rows: int) -> np.ndarray:
+def zipf_ranks(n: int, theta: float, seed: int, rows: int, start: int = 0) -> np.ndarray:
     """Zipf(theta) ranks in [1, n] by rejection-inversion (Hoermann & Derflinger
-    1996); attempt j of row i draws rand64(seed, 4, i*64 + j)."""
+    1996); attempt j of row i draws rand64(seed, 4, i*64 + j).  Rows
+    [start, start + rows)."""
     s = float(theta)
     h_x1 = float(_zh_integral(s, np.array([1.5]))[0] - 1.0)
     h_n = float(_zh_integral(s, np.array([n + 0.5]))[0])
     s_const = float(2.0 - _zh_integral_inv(s, _zh_integral(s, np.array([2.5])) - _zh(s, np.array([2.0])))[0])
-    idx = np.arange(rows, dtype=np.uint64)
+    idx = np.arange(start, start + rows, dtype=np.uint64)
     out = np.ones(rows, dtype=np.uint64)
     pending = np.ones(rows, dtype=bool)
     for attempt in range(64):
@@ -172,14 +176,54 @@ def zipf_ranks(n: int, theta: float, seed: int, rows: int) -> np.ndarray:
         x = _zh_integral_inv(s, u)
         kd = np.clip(np.floor(x + 0.5), 1.0, float(n))
         acc = (kd - x <= s_const) | (u >= _zh_integral(s, kd + 0.5) - _zh(s, kd))
-        out[ii] = kd.astype(np.uint64)
-        done = ii[acc]
-        pending[done] = False
+        pos = (ii - np.uint64(start)).astype(np.int64)
+        out[pos] = kd.astype(np.uint64)
+        pending[pos[acc]] = False
     return out
 
 
-def gen_zipf_keys(rows: int, seed: int, key_seed: int, domain: int, theta: float = 1.0) -> np.ndarray:
+def gen_zipf_keys(rows: int, seed: int, key_seed: int, domain: int, theta: float = 1.0, start: int = 0) -> np.ndarray:
     """Kind 5: Zipf ranks mapped through a seeded permutation onto K(0..domain-1)."""
-    ranks = zipf_ranks(domain, theta, seed, rows)
+    ranks = zipf_ranks(domain, theta, seed, rows, start)
     perm = Perm(domain, seed ^ 0x2545F4914F6CDD1D)
     return key_of(key_seed, perm(ranks - np.uint64(1)))
+
+
+def parallel_rows(rows: int, make, dtype, width: int = 1, threads: int = 0) -> np.ndarray:
+    """Fills an array of `rows` rows from make(start, n) -> rows [start,
+    start + n), in chunks on a thread pool (numpy's arithmetic releases the
+    interpreter lock): the same integers as one make(0, rows) call."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    threads = threads or min(32, os.cpu_count() or 1)
+    shape = (rows,) if width == 1 else (rows, width)
+    out = np.empty(shape, dtype=dtype)
+    step = max(1 << 20, -(-rows // (4 * threads)))
+
+    def fill(lo):
+        n = min(step, rows - lo)
+        out[lo:lo + n] = make(lo, n)
+
+    with ThreadPoolExecutor(threads) as ex:
+        list(ex.map(fill, range(0, rows, step)))
+    return out
+
+
+def parallel_keys(kind: int, rows: int, seed: int, key_seed: int, domain: int = 0, match_permille: int = 1000,
+                  theta: float = 1.0, threads: int = 0) -> np.ndarray:
+    """gen_keys (kinds 0, 1, 3, 4) or gen_zipf_keys (kind 5) in parallel chunks."""
+    if kind == 5:
+        return parallel_rows(rows, lambda lo, n: gen_zipf_keys(n, seed, key_seed, domain, theta, start=lo), np.uint64, threads=threads)
+    return parallel_rows(rows, lambda lo, n: gen_keys(kind, n, seed, key_seed, domain, match_permille, start=lo, total=rows),
+                         np.uint64, threads=threads)
+
+
+def parallel_payloads(seed: int, types: Sequence[int], rows: int, threads: int = 0) -> List[np.ndarray]:
+    """payload_columns in parallel chunks."""
+    cols = []
+    for c, t in enumerate(types):
+        def make(lo, n, c=c, t=t):
+            return payload_columns(seed, [U8] * c + [t], n, start=lo)[c]
+        cols.append(parallel_rows(rows, make, np.uint64 if t == U128 else _DT[t], width=2 if t == U128 else 1, threads=threads))
+    return cols
