@@ -278,20 +278,71 @@ def cpu_budget_mib(workload, threads):
     return BEP_BUDGET_PER_GROUP.get(workload, 32) * threads
 
 
+def sample_text(build_rows, n_p, probe_rows, scheme, threads, runs, stat):
+    """What the CPU runs covered, for the JSON line."""
+    part = "the whole workload" if n_p == probe_rows else f"the full build side and the first {n_p} of {probe_rows} probe rows"
+    import platform
+    arch = platform.machine()
+    simd = ("the scalar intHash64Batch, the reference's path on a host without AVX-512 (src/Hash.h:35-58)" if arch in ("aarch64", "arm64")
+            else "a scalar intHash64Batch (the reference would take its AVX-512 path here, src/Hash.h:35-58)")
+    return (f"{scheme} on {part} ({build_rows} + {n_p} rows); {stat} of {runs} runs on {threads} threads of this {arch} host; C++ port "
+            f"of the reference's scheme (oracle/cpu_port.cpp; the reference's sources are not on this machine) with {simd}")
+
+
 def cpu_baseline(bhost, phost, bits, frac, threads, scheme, reps=3, budget_mib=512):
     import oracle
     n_p = max(1, int(len(phost.keys) * frac))
-    probe = type(phost)(phost.types, phost.keys[:n_p], [c[:n_p] for c in phost.payloads])
+    probe = phost if n_p == len(phost.keys) else type(phost)(phost.types, phost.keys[:n_p], [c[:n_p] for c in phost.payloads])
     times = []
     for _ in range(reps):
         _, ms = oracle.port_run(scheme, bhost, probe, bits, threads, budget_mib)
         times.append(ms["e2e"])
     t = statistics.median(times) / 1e3
     return {"value": (len(bhost.keys) + n_p) / t, "unit": "tuples/s", "cores": threads, "kind": "port",
-            "sample": f"{scheme} on the full build side ({len(bhost.keys)} rows) and the first {n_p} probe rows "
-                      f"({frac:.4g} of the probe side); median of {reps} runs, {threads} host threads; "
-                      f"C++ port of the reference's scheme (oracle/cpu_port.cpp)",
+            "sample": sample_text(len(bhost.keys), n_p, len(phost.keys), scheme, threads, reps, "median"),
             "ms_per_run": statistics.median(times)}
+
+
+def host_tables(wl, probe_rows=None):
+    """The workload's build and probe sides generated on the host (the same
+    integers as the device generator, phj_table_generate), optionally only
+    the first `probe_rows` probe rows."""
+    import phj_datagen as G
+    import phj_gpu as P
+    _, _, bspec, pspec, _ = WORKLOADS[wl]
+    if bspec["kind"] == 2:
+        bk, used = G.gen_multi_match_keys(bspec["rows"], bspec["seed"], bspec["key_seed"])
+    else:
+        bk, used = G.parallel_keys(bspec["kind"], bspec["rows"], bspec["seed"], bspec["key_seed"]), bspec["rows"]
+    b = P.BlockStream(bspec["types"], bk, G.parallel_payloads(bspec["seed"], bspec["types"], bspec["rows"]))
+    n_p = pspec["rows"] if probe_rows is None else probe_rows
+    dom = pspec.get("domain") or used
+    pk = G.parallel_keys(pspec["kind"], n_p, pspec["seed"], pspec["key_seed"], domain=dom,
+                         match_permille=pspec.get("match_permille", 1000), theta=pspec.get("theta", 1.0))
+    return b, P.BlockStream(pspec["types"], pk, G.parallel_payloads(pspec["seed"], pspec["types"], n_p))
+
+
+def golden_fingerprint(wl):
+    """The oracle's fingerprint of a full-size workload's join, as
+    tests/golden/gen_fullsize.py recorded it (None if absent)."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "tests", "golden", "fullsize.json")))
+        return tuple(int(v) for v in d[wl]["fingerprint"])
+    except Exception:
+        return None
+
+
+def workload_config(desc, scheme, build_rows, probe_rows, output_rows, bits, probe_types, world, n_p=None):
+    """The `config` object of both arms' JSON lines: the same workload gives
+    the same object on the GPU and on the host cores."""
+    cfg = {"workload": desc, "scheme": scheme, "build_rows": build_rows, "probe_rows": probe_rows if n_p is None else n_p,
+           "output_rows": output_rows, "radix_pass_bits": list(bits),
+           "l2": f"probe side {probe_rows * row_bytes(probe_types) / 1e9:.2f} GB; an L2 flush (a write larger than L2) between steps"}
+    if n_p is not None and n_p != probe_rows:
+        cfg["probe_sample_of"] = probe_rows
+    if world > 1:
+        cfg["parallelism"] = f"{world} replicas"
+    return cfg
 
 
 def host_streams_from_device(ctx, b, p):
@@ -303,36 +354,35 @@ def reference_arm(args, rank, world, dist):
     if rank != 0:
         return
     import oracle
-    import phj_datagen as G
     import phj_gpu as P
+    if args.scale != 1.0:
+        scale_workload(args.workload, args.scale)
     desc, scheme, bspec, pspec, bits = WORKLOADS[args.workload]
+    scheme = args.scheme or scheme
     threads = os.cpu_count() or 1
     frac = args.cpu_probe_frac
     if args.pass_bits:
         bits = [int(x) for x in args.pass_bits.split(",")]
     if bits is None:
         bits = P.autotune_radix(bspec["rows"])
-    if bspec["kind"] == 2:
-        bk, used = G.gen_multi_match_keys(bspec["rows"], bspec["seed"], bspec["key_seed"])
-    else:
-        bk, used = G.gen_keys(bspec["kind"], bspec["rows"], bspec["seed"], bspec["key_seed"]), bspec["rows"]
-    b = P.BlockStream(bspec["types"], bk, G.payload_columns(bspec["seed"], bspec["types"], bspec["rows"]))
+    # the same seeded inputs as the GPU arm's device generator, made on the
+    # host in parallel chunks (not timed)
     n_p = max(1, int(pspec["rows"] * frac))
-    dom = pspec.get("domain") or used
-    if pspec["kind"] == 4:
-        pk = G.gen_keys(4, n_p, pspec["seed"], pspec["key_seed"], domain=dom, match_permille=pspec["match_permille"])
-    elif pspec["kind"] == 5:
-        pk = G.gen_zipf_keys(n_p, pspec["seed"], pspec["key_seed"], dom, pspec.get("theta", 1.0))
-    else:
-        pk = G.gen_keys(pspec["kind"], n_p, pspec["seed"], pspec["key_seed"], domain=dom)
-    p = P.BlockStream(pspec["types"], pk, G.payload_columns(pspec["seed"], pspec["types"], n_p))
+    b, p = host_tables(args.workload, n_p)
     cs = scheme
     budget = cpu_budget_mib(args.workload, threads)
-    for _ in range(args.warmup):
+    # one untimed run checks the port's rows against the oracle's answer for
+    # the full workload (tests/golden/fullsize.json)
+    _, ms = oracle.port_run(cs, b, p, bits, threads, budget, fingerprint=True)
+    checked = None
+    golden = golden_fingerprint(args.workload)
+    if golden is not None and n_p == pspec["rows"] and args.scale == 1.0:
+        checked = tuple(ms["fingerprint"]) == golden
+    for _ in range(max(0, args.warmup - 1)):
         oracle.port_run(cs, b, p, bits, threads, budget)
     times = []
     for _ in range(args.steps):
-        _, ms = oracle.port_run(cs, b, p, bits, threads, budget)
+        out_rows, ms = oracle.port_run(cs, b, p, bits, threads, budget)
         times.append(ms["e2e"])
     t = statistics.mean(times)
     value = (len(b.keys) + n_p) / (t / 1e3)
@@ -340,12 +390,11 @@ def reference_arm(args, rank, world, dist):
         "impl": "reference", "metric": "join tuples/s (build+probe)", "value": value, "unit": "tuples/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64", "data": "synthetic (seeded, same generator specification as the GPU arm)",
-        "config": {"workload": desc, "scheme": scheme, "build_rows": len(b.keys), "probe_rows": n_p,
-                   "probe_sample_of": pspec["rows"], "radix_pass_bits": bits},
+        "config": workload_config(desc, scheme, len(b.keys), pspec["rows"], int(out_rows), bits, pspec["types"], world, n_p),
         "cpu_baseline": {"value": value, "unit": "tuples/s", "cores": threads, "kind": "port",
-                         "sample": f"full build side, first {n_p} of {pspec['rows']} probe rows; C++ port of the reference's "
-                                   f"{cs} (oracle/cpu_port.cpp) because the reference sources are not on this machine"},
+                         "sample": sample_text(len(b.keys), n_p, pspec["rows"], cs, threads, args.steps, "mean")},
         "e2e": {"value": value, "unit": "tuples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "output_equals_oracle": checked,
     }
     print(json.dumps(line), flush=True)
 
@@ -361,7 +410,7 @@ def main():
     ap.add_argument("--bep-budget-mib", type=int, default=0, help="PHJ (BEP) whole-run probe budget (default: per-group budget x SMs)")
     ap.add_argument("--pass-bits", default=None, help="radix bits per pass, e.g. 8,8 (overrides the workload's; no autotuning)")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--cpu-probe-frac", type=float, default=1 / 16)
+    ap.add_argument("--cpu-probe-frac", type=float, default=1.0, help="fraction of the probe side the CPU runs take (default: all of it)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-chj", action="store_true")
@@ -462,11 +511,8 @@ def main():
         "metric": "join tuples/s (build+probe)", "value": value, "unit": "tuples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u64", "data": "synthetic (seeded device generator; keys, payloads and match rate as specified)",
-        "config": {"workload": desc, "scheme": scheme, "build_rows": B, "probe_rows": Pn, "radix_pass_bits": bits,
-                   "output_rows": out_rows,
-                   "l2": f"inputs larger than L2 (probe side {Pn * row_bytes(pspec['types']) / 1e9:.1f} GB) and an L2 flush between steps",
-                   "parallelism": "replicas" if world > 1 else "single GPU", "options": args.set,
-                   "autotuned": tuned},
+        "config": workload_config(desc, scheme, B, Pn, out_rows, bits, pspec["types"], world),
+        "tuning": {"options": args.set, "autotuned": tuned},
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": profiled_traffic(dom_name, args.workload, args.scale),
                      "bytes_per_launch": bytes_per_launch, "ms_per_launch": avg_ms, "launches_timed": dom["launches"],
@@ -481,8 +527,9 @@ def main():
     }
 
     if scheme == "phj":
-        line["config"]["bep_budget_mib"] = budget
         line["bep"] = {k: getattr(res, k) for k in ("bep_evictions", "bep_refinements", "bep_peak_bytes", "bep_build_skip_retries")}
+        line["bep"]["budget_mib"] = budget
+        line["bep"]["budget_mib_per_group"] = BEP_BUDGET_PER_GROUP.get(args.workload, 32)
         line["bep"]["phase_ms"] = {k: getattr(res, k).wall_ms for k in
                                    ("build_shuffle", "build", "probe_shuffle", "probe", "eviction_overhead")}
 

@@ -3,6 +3,7 @@
 // compiled.  Test and measurement infrastructure only, never on the device
 // path.  See cpu_port.h for the reference file:line map.
 #include "cpu_port.h"
+#include "oracle.h"
 
 #include <algorithm>
 #include <atomic>
@@ -440,10 +441,36 @@ Schema schema_of(const port_stream & s)
         sc.w.push_back(width_of(s.types[c]));
     return sc;
 }
+
+// The order-independent fingerprint of every materialised output row (the
+// oracle's, oracle_columns_fingerprint: row count and two sums of per-row
+// hashes), taken after the timed region so the check costs the timing
+// nothing.
+void fingerprint_outputs(const std::vector<Materialiser> & mats, const port_stream & b, const port_stream & p, uint64_t * fp)
+{
+    if (!fp)
+        return;
+    fp[0] = fp[1] = fp[2] = 0;
+    for (const Materialiser & m : mats)
+        for (const OutputBlock & blk : m.done)
+        {
+            const void * l[8] = {};
+            const void * r[8] = {};
+            for (size_t c = 0; c < blk.left.size(); ++c)
+                l[c] = blk.left[c].data();
+            for (size_t c = 0; c < blk.right.size(); ++c)
+                r[c] = blk.right[c].data();
+            uint64_t f[3];
+            oracle_columns_fingerprint(blk.rows, blk.keys.data(), b.n_payloads, b.types, l, p.n_payloads, p.types, r, f);
+            fp[0] += f[0];
+            fp[1] += f[1];
+            fp[2] += f[2];
+        }
+}
 } // namespace
 
 extern "C" int64_t port_run_phj_pure(const port_stream * build, const port_stream * probe, const uint8_t * pass_bits, uint32_t n_passes,
-                                     uint32_t threads, double * phase_ms)
+                                     uint32_t threads, double * phase_ms, uint64_t * fp)
 {
     if (!build || !probe || !pass_bits || n_passes == 0)
         return -1;
@@ -502,6 +529,7 @@ extern "C" int64_t port_run_phj_pure(const port_stream * build, const port_strea
         phase_ms[3] = *std::max_element(probe_ms.begin(), probe_ms.end());
         phase_ms[4] = e2e;
     }
+    fingerprint_outputs(mats, *build, *probe, fp);
     return total;
 }
 
@@ -516,7 +544,7 @@ struct Slot
 };
 } // namespace
 
-extern "C" int64_t port_run_chj(const port_stream * build, const port_stream * probe, uint32_t threads, double * phase_ms)
+extern "C" int64_t port_run_chj(const port_stream * build, const port_stream * probe, uint32_t threads, double * phase_ms, uint64_t * fp)
 {
     if (!build || !probe)
         return -1;
@@ -642,6 +670,7 @@ extern "C" int64_t port_run_chj(const port_stream * build, const port_stream * p
         phase_ms[1] = t_probe;
         phase_ms[2] = ms_since(t0);
     }
+    fingerprint_outputs(mats, *build, *probe, fp);
     return total;
 }
 
@@ -696,7 +725,7 @@ void refine_chain(std::vector<OutBlk> && in, const Schema & s, const std::vector
 } // namespace
 
 extern "C" int64_t port_run_phj_bep(const port_stream * build, const port_stream * probe, const uint8_t * pass_bits, uint32_t n_passes,
-                                    uint32_t threads, uint64_t budget_mib, double * phase_ms, uint64_t * counters)
+                                    uint32_t threads, uint64_t budget_mib, double * phase_ms, uint64_t * counters, uint64_t * fp)
 {
     if (!build || !probe || !pass_bits || n_passes == 0 || budget_mib == 0)
         return -1;
@@ -945,5 +974,6 @@ extern "C" int64_t port_run_phj_bep(const port_stream * build, const port_stream
         counters[2] = peak.load();
         counters[3] = skips.load();
     }
+    fingerprint_outputs(mats, *build, *probe, fp);
     return total;
 }

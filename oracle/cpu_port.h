@@ -32,18 +32,20 @@ typedef struct port_stream {
 } port_stream;
 
 /* phase_ms: [0] build_shuffle, [1] build, [2] probe_shuffle, [3] probe, [4] e2e.
- * Returns output rows (materialised, then dropped), or -1 on bad arguments. */
+ * Returns output rows (materialised, then dropped), or -1 on bad arguments.
+ * fp, when not NULL, receives the oracle's order-independent fingerprint of
+ * the materialised rows (oracle_columns_fingerprint), taken after timing. */
 int64_t port_run_phj_pure(const port_stream *build, const port_stream *probe, const uint8_t *pass_bits, uint32_t n_passes,
-                          uint32_t threads, double *phase_ms);
+                          uint32_t threads, double *phase_ms, uint64_t *fp);
 
 /* phase_ms: [0] build_shuffle, [1] build, [2] probe_shuffle, [3] probe,
  * [4] eviction_overhead, [5] e2e; counters: [0] evictions, [1] refinements,
  * [2] peak buffered leaf bytes, [3] skipped try-locks. */
 int64_t port_run_phj_bep(const port_stream *build, const port_stream *probe, const uint8_t *pass_bits, uint32_t n_passes,
-                         uint32_t threads, uint64_t budget_mib, double *phase_ms, uint64_t *counters);
+                         uint32_t threads, uint64_t budget_mib, double *phase_ms, uint64_t *counters, uint64_t *fp);
 
 /* phase_ms: [0] build, [1] probe, [2] e2e. */
-int64_t port_run_chj(const port_stream *build, const port_stream *probe, uint32_t threads, double *phase_ms);
+int64_t port_run_chj(const port_stream *build, const port_stream *probe, uint32_t threads, double *phase_ms, uint64_t *fp);
 
 #ifdef __cplusplus
 }

@@ -254,13 +254,14 @@ def port():
             subprocess.run(["make", "-s", "-C", HERE, "libcpuport.so"], check=True)
         L = C.CDLL(path)
         S = C.POINTER(PortStream)
+        FP = C.POINTER(C.c_uint64)
         L.port_run_phj_pure.restype = C.c_int64
-        L.port_run_phj_pure.argtypes = [S, S, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32, C.POINTER(C.c_double)]
+        L.port_run_phj_pure.argtypes = [S, S, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32, C.POINTER(C.c_double), FP]
         L.port_run_chj.restype = C.c_int64
-        L.port_run_chj.argtypes = [S, S, C.c_uint32, C.POINTER(C.c_double)]
+        L.port_run_chj.argtypes = [S, S, C.c_uint32, C.POINTER(C.c_double), FP]
         L.port_run_phj_bep.restype = C.c_int64
         L.port_run_phj_bep.argtypes = [S, S, C.POINTER(C.c_uint8), C.c_uint32, C.c_uint32, C.c_uint64, C.POINTER(C.c_double),
-                                       C.POINTER(C.c_uint64)]
+                                       C.POINTER(C.c_uint64), FP]
         _port = L
     return _port
 
@@ -278,26 +279,33 @@ def port_stream(s, block_rows: int = 10_000) -> PortStream:
     return o
 
 
-def port_run(scheme: str, build, probe, pass_bits=(8,), threads: int = 0, budget_mib: int = 512):
+def port_run(scheme: str, build, probe, pass_bits=(8,), threads: int = 0, budget_mib: int = 512, fingerprint: bool = False):
     """Times the CPU port of the reference's runPHJ ('phj-pure'), runCHJ
     ('chj') or runPhjBep ('phj').  Returns (output rows, phase ms dict);
-    for 'phj' the dict also holds the BEP counters."""
+    for 'phj' the dict also holds the BEP counters.  With `fingerprint` the
+    dict holds the oracle fingerprint of the rows the port materialised
+    (computed after the timed region)."""
     threads = threads or (os.cpu_count() or 1)
     ms = (C.c_double * 6)()
+    fp = (C.c_uint64 * 3)() if fingerprint else None
     b, p = port_stream(build), port_stream(probe)
     if scheme == "phj-pure":
         bits = (C.c_uint8 * len(pass_bits))(*pass_bits)
-        n = port().port_run_phj_pure(C.byref(b), C.byref(p), bits, len(pass_bits), threads, ms)
-        return n, {"build_shuffle": ms[0], "build": ms[1], "probe_shuffle": ms[2], "probe": ms[3], "e2e": ms[4]}
-    if scheme == "phj":
+        n = port().port_run_phj_pure(C.byref(b), C.byref(p), bits, len(pass_bits), threads, ms, fp)
+        d = {"build_shuffle": ms[0], "build": ms[1], "probe_shuffle": ms[2], "probe": ms[3], "e2e": ms[4]}
+    elif scheme == "phj":
         bits = (C.c_uint8 * len(pass_bits))(*pass_bits)
         ctr = (C.c_uint64 * 4)()
-        n = port().port_run_phj_bep(C.byref(b), C.byref(p), bits, len(pass_bits), threads, budget_mib, ms, ctr)
-        return n, {"build_shuffle": ms[0], "build": ms[1], "probe_shuffle": ms[2], "probe": ms[3], "eviction_overhead": ms[4],
-                   "e2e": ms[5], "bep_evictions": ctr[0], "bep_refinements": ctr[1], "bep_peak_bytes": ctr[2],
-                   "bep_build_skip_retries": ctr[3]}
-    n = port().port_run_chj(C.byref(b), C.byref(p), threads, ms)
-    return n, {"build": ms[0], "probe": ms[1], "e2e": ms[2]}
+        n = port().port_run_phj_bep(C.byref(b), C.byref(p), bits, len(pass_bits), threads, budget_mib, ms, ctr, fp)
+        d = {"build_shuffle": ms[0], "build": ms[1], "probe_shuffle": ms[2], "probe": ms[3], "eviction_overhead": ms[4],
+             "e2e": ms[5], "bep_evictions": ctr[0], "bep_refinements": ctr[1], "bep_peak_bytes": ctr[2],
+             "bep_build_skip_retries": ctr[3]}
+    else:
+        n = port().port_run_chj(C.byref(b), C.byref(p), threads, ms, fp)
+        d = {"build": ms[0], "probe": ms[1], "e2e": ms[2]}
+    if fingerprint:
+        d["fingerprint"] = (fp[0], fp[1], fp[2])
+    return n, d
 
 
 def ref_time(scheme: str, build, probe, pass_bits=(8,), threads: int = 0, budget_mib: int = 512):
