@@ -183,7 +183,7 @@ phj_status phj_ctx_set_int(phj_ctx *ctx, const char *name, int64_t value);
  * "l2_bytes", "wait_limit_ms". */
 phj_status phj_ctx_get_int(const phj_ctx *ctx, const char *name, int64_t *value);
 
-/* ---- radix configuration: CLI.cpp:376-408 ------------------------------ */
+/* ---- radix configuration: src/CLI.cpp:330-355 ---------------------------- */
 
 /* Resolves --partitions/--passes (or an explicit --partition-bits-per-pass
  * list when n_bits_override > 0) into per-pass bits exactly as the
@@ -229,6 +229,19 @@ uint64_t phj_table_rows(const phj_table *t);
 /* Distinct keys of a table generated with kind 0 or 2 (0 otherwise). */
 uint64_t phj_table_gen_distinct(const phj_table *t);
 void phj_table_free(phj_ctx *ctx, phj_table *t);
+
+/* ---- the radix partition operator ------------------------------------------ */
+
+/* radixShuffle(input, cfg, threads) (src/RadixPartition.h:198-199,
+ * src/RadixPartition.cpp:546-586): partitions `input` by the top
+ * sum(pass_bits) bits of intHash64(key), pass by pass as the reference does,
+ * into a new device table whose rows are in partition order, one block per
+ * partition (PartitionedShuffleOutput::chains[p]).  partition_rows, when not
+ * NULL, receives the 2^sum(pass_bits) row counts
+ * (PartitionedShuffleOutput::partition_rows).  Rows keep their payloads; the
+ * order of rows inside a partition is unspecified, as in the reference. */
+phj_status phj_radix_shuffle(phj_ctx *ctx, const phj_table *input, const uint8_t *pass_bits, uint32_t n_passes,
+                             phj_table **out, uint64_t *partition_rows);
 
 /* ---- the three schemes ---------------------------------------------------- */
 
@@ -356,9 +369,12 @@ uint64_t phj_serve_footprint(const phj_serve_request *r, int batched);
  * `out_right[probe payloads]`) of `out_capacity` rows, in no particular
  * order.  `*out_rows` receives the join's row count; above the capacity the
  * call returns PHJ_ERR_CAPACITY with the first `out_capacity` rows written.
- * The first call on a device sets up (it resolves the scratch address), so
- * make it before capturing a stream.  Calls that overlap in time on one
- * device race on the shared scratch: serialise them. */
+ * The first call on a device sets up (it resolves the scratch address):
+ * make that first call before any stream capture.  Every call waits for its
+ * context's stream before it returns (it reads the row count back), and its
+ * kernels are recorded for phj_last_kernel_times.  With out_capacity 0 the
+ * column arrays may be NULL: the call only counts.  Calls that overlap in
+ * time on one device race on the shared scratch: serialise them. */
 phj_status phj_run_chj_noalloc(phj_ctx *ctx, const phj_table *build, const phj_table *probe, uint64_t out_capacity,
                                uint64_t *out_keys, void *const *out_left, void *const *out_right, uint64_t *out_rows);
 

@@ -1821,6 +1821,50 @@ phj_status phj_run_phj_pure(phj_ctx * ctx, const phj_table * build, const phj_ta
     });
 }
 
+phj_status phj_radix_shuffle(phj_ctx * ctx, const phj_table * input, const uint8_t * pass_bits, uint32_t n_passes, phj_table ** out,
+                             uint64_t * partition_rows)
+{
+    if (!ctx || !input || !out)
+        return PHJ_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    return guard(ctx, [&] {
+        const std::vector<uint32_t> bits = check_bits(pass_bits, n_passes);
+        if (input->rows >= (1ull << 32))
+            throw Error(PHJ_ERR_UNSUPPORTED, "the device radix shuffle takes < 2^32 rows");
+        uint32_t total_bits = 0;
+        for (uint32_t b : bits)
+            total_bits += b;
+        const uint64_t n_parts = 1ull << total_bits;
+        begin_run(ctx);
+        Scratch s(ctx);
+        phj_table * t = alloc_table(ctx, input->schema, input->rows);
+        try
+        {
+            const Cols tmp = alloc_cols_like(s, input->schema, input->rows);
+            uint32_t * leaf_off = s.get<uint32_t>(n_parts + 1);
+            radix_partition(ctx, s, cols_of(*input), input->rows, bits, cols_of(*t), tmp, leaf_off, "radix_shuffle");
+            // one block per partition (PartitionedShuffleOutput::chains[p])
+            std::vector<uint32_t> off(n_parts + 1);
+            PHJ_CUDA(cudaMemcpyAsync(off.data(), leaf_off, (n_parts + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+            PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+            std::vector<uint32_t> rows(n_parts);
+            for (uint64_t p = 0; p < n_parts; ++p)
+            {
+                rows[p] = off[p + 1] - off[p];
+                if (partition_rows)
+                    partition_rows[p] = rows[p];
+            }
+            set_block_structure(ctx, t, (uint32_t)n_parts, rows.data()); // at most 2^24 partitions
+        }
+        catch (...)
+        {
+            free_table(ctx, t);
+            throw;
+        }
+        *out = t;
+    });
+}
+
 phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_table * probe, const uint8_t * pass_bits, uint32_t n_passes,
                            uint64_t bep_budget_mib, uint32_t workers, phj_output ** out, phj_bep_result * result)
 {

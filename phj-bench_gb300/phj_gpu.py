@@ -35,7 +35,7 @@ STATUS = {
     0: "PHJ_OK", 1: "PHJ_ERR_INVALID_ARGUMENT", 2: "PHJ_ERR_CUDA", 3: "PHJ_ERR_OUT_OF_MEMORY",
     4: "PHJ_ERR_UNSUPPORTED", 5: "PHJ_ERR_DEVICE_TIMEOUT", 6: "PHJ_ERR_NO_DEVICE", 7: "PHJ_ERR_CAPACITY",
 }
-ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_DEVICE_TIMEOUT = 1, 2, 5
+ERR_INVALID_ARGUMENT, ERR_CUDA, ERR_DEVICE_TIMEOUT, ERR_CAPACITY = 1, 2, 5, 7
 
 
 class PhjError(RuntimeError):
@@ -137,6 +137,7 @@ def load() -> C.CDLL:
         "phj_table_wrap_device": (C.c_int, [P, C.POINTER(BlockStreamDesc), C.POINTER(P)]),
         "phj_table_generate": (C.c_int, [P, C.POINTER(GenSpec), C.POINTER(P)]),
         "phj_table_download": (C.c_int, [P, P, P, C.POINTER(C.c_void_p)]),
+        "phj_radix_shuffle": (C.c_int, [P, P, C.POINTER(C.c_uint8), C.c_uint32, C.POINTER(P), P]),
         "phj_table_rows": (C.c_uint64, [P]),
         "phj_table_gen_distinct": (C.c_uint64, [P]),
         "phj_table_free": (None, [P, P]),
@@ -184,7 +185,7 @@ def load() -> C.CDLL:
 
 
 def resolve_radix(partitions: int = 256, passes: int = 1, bits_per_pass: Optional[Sequence[int]] = None) -> List[int]:
-    """--partitions / --passes / --partition-bits-per-pass resolution (src/CLI.cpp:376-408)."""
+    """--partitions / --passes / --partition-bits-per-pass resolution (src/CLI.cpp:330-355)."""
     lib = load()
     out = (C.c_uint8 * 32)()
     n = C.c_uint32()
@@ -493,6 +494,17 @@ class Context:
         h = C.c_void_p()
         self._check(self.lib.phj_table_generate(self.ptr, C.byref(sp), C.byref(h)))
         return Table(self, h, types)
+
+    # ---- the radix partition operator ----
+    def radix_shuffle(self, table: Table, pass_bits: Sequence[int]):
+        """radixShuffle (src/RadixPartition.cpp:546-586) on the device:
+        returns (the partitioned Table, rows of every partition)."""
+        bits = (C.c_uint8 * max(1, len(pass_bits)))(*pass_bits)
+        counts = np.zeros(1 << min(24, sum(pass_bits)), dtype=np.uint64) if sum(pass_bits) <= 24 else None
+        h = C.c_void_p()
+        self._check(self.lib.phj_radix_shuffle(self.ptr, table.handle, bits, len(pass_bits), C.byref(h),
+                                               counts.ctypes.data if counts is not None else None))
+        return Table(self, h, table.types), counts
 
     # ---- schemes ----
     def run_chj(self, build: Table, probe: Table):

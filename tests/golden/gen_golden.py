@@ -59,6 +59,12 @@ def main():
         n = R.ref_radix_shuffle_keys(O.C.byref(O.ostream(b)), 10000, arr, len(bits), 3, prow.ctypes.data, keys.ctypes.data)
         assert n == len(b.keys)
         out["kat"]["radix_partition_rows_c2_mini_" + "_".join(map(str, bits))] = [int(v) for v in prow]
+        # the keys of each partition as a multiset: sorted inside each
+        # partition, partitions in order (the order inside a partition
+        # depends on the reference's threads)
+        offs = np.concatenate([[0], np.cumsum(prow)]).astype(np.int64)
+        per_part = np.concatenate([np.sort(keys[offs[i]:offs[i + 1]]) for i in range(parts)])
+        out["kat"]["radix_partition_keys_sha256_c2_mini_" + "_".join(map(str, bits))] = hashlib.sha256(per_part.tobytes()).hexdigest()
     with open(os.path.join(HERE, "golden.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("wrote", os.path.join(HERE, "golden.json"))

@@ -1,6 +1,6 @@
 """Host-side checks of the C ABI that need no GPU: the library loads, it
 exports every function include/phj_gpu.h declares, and the radix
-configuration resolves as the reference CLI does (src/CLI.cpp:376-408)."""
+configuration resolves as the reference CLI does (src/CLI.cpp:330-355)."""
 import ctypes
 import os
 import re
@@ -122,6 +122,7 @@ def test_entry_points_reject_a_null_context_without_a_device(lib):
                                                                  keys, ptrs, ptrs, ctypes.byref(rows), None),
         "phj_run_chj_noalloc": lambda: lib.phj_run_chj_noalloc(None, None, None, 0, None, None, None, ctypes.byref(rows)),
         "phj_batch_run": lambda: lib.phj_batch_run(None, 0, None, None, None, None),
+        "phj_radix_shuffle": lambda: lib.phj_radix_shuffle(None, None, None, 0, ctypes.byref(out), None),
         "phj_table_generate": lambda: lib.phj_table_generate(None, None, ctypes.byref(out)),
         "phj_table_upload": lambda: lib.phj_table_upload(None, ctypes.byref(desc), ctypes.byref(out)),
         "phj_output_fingerprint": lambda: lib.phj_output_fingerprint(None, None, keys),

@@ -42,6 +42,22 @@ def test_leaf_ids_match_reference_radix_shuffle(bits):
     assert got.tolist() == want
 
 
+def partition_key_digest(keys, leaf, parts):
+    """sha256 of the keys grouped by partition, sorted inside each one."""
+    import hashlib
+    order = np.lexsort((keys, leaf))
+    assert np.all(np.diff(leaf[order].astype(np.int64)) >= 0) and leaf.max(initial=0) < parts
+    return hashlib.sha256(np.ascontiguousarray(keys[order]).tobytes()).hexdigest()
+
+
+@pytest.mark.parametrize("bits", [[4], [3, 3], [2, 2, 2]])
+def test_leaf_ids_place_every_key_where_radix_shuffle_does(bits):
+    b, _ = cases.make("c2_mini")
+    want = GOLDEN["kat"]["radix_partition_keys_sha256_c2_mini_" + "_".join(map(str, bits))]
+    leaf = O.leaf_ids(b.keys, sum(bits))
+    assert partition_key_digest(b.keys, leaf, 1 << sum(bits)) == want
+
+
 def test_compare_detects_a_planted_mistake():
     b, p = cases.make("c2_mini")
     rows = O.join_rows(b, p)
