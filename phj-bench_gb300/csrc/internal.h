@@ -346,15 +346,32 @@ void set_build_smem_limits(int smem_optin);
 // device back afterwards: a context may be used from any host thread (the
 // request loop's workers are threads of their own) whatever device that
 // thread has current.
+// A device that cannot be made current is recorded in `err` (the calls
+// then fail with PHJ_ERR_CUDA before any launch); an error the caller had
+// pending is left as it was unless one of these calls failed.
 struct DeviceScope
 {
     int prev = -1;
+    cudaError_t err = cudaSuccess;
     explicit DeviceScope(const phj_ctx * ctx)
     {
+        if (!ctx)
+            return;
         int cur = -1;
-        if (ctx && cudaGetDevice(&cur) == cudaSuccess && cur != ctx->device && cudaSetDevice(ctx->device) == cudaSuccess)
-            prev = cur;
-        cudaGetLastError();
+        err = cudaGetDevice(&cur);
+        if (err == cudaSuccess && cur != ctx->device)
+        {
+            err = cudaSetDevice(ctx->device);
+            if (err == cudaSuccess)
+                prev = cur;
+        }
+        if (err != cudaSuccess)
+            cudaGetLastError(); // the error just recorded, not the caller's
+    }
+    bool ok() const { return err == cudaSuccess; }
+    std::string message(const phj_ctx * ctx) const
+    {
+        return "cannot make device " + std::to_string(ctx ? ctx->device : -1) + " current: " + cudaGetErrorString(err);
     }
     ~DeviceScope()
     {
@@ -371,6 +388,12 @@ template <class F>
 inline phj_status guard(phj_ctx * ctx, F && f)
 {
     DeviceScope dev(ctx);
+    if (!dev.ok())
+    {
+        if (ctx)
+            ctx->last_error = dev.message(ctx);
+        return PHJ_ERR_CUDA;
+    }
     try
     {
         f();

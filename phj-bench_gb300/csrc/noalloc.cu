@@ -160,28 +160,36 @@ void run_chj_noalloc(phj_ctx * ctx, const phj_table & B, const phj_table & P, ui
         if (out_cap > 0 && (!out_right || !out_right[c]))
             throw Error(PHJ_ERR_INVALID_ARGUMENT, "no-allocation join: probe payload output column missing");
 
+    begin_run(ctx); // this call's kernel times replace the previous run's
     const NaScratch s = carve(scratch_address(ctx->device));
     const uint64_t cap = B.rows ? bit_ceil64(2 * B.rows) : 1;
     const Cols bc = cols_of(B), pc = cols_of(P);
     Cols ol = bc, orr = pc;
     ol.keys = out_keys;
     orr.keys = nullptr;
+    // a caller asking only for the row count (capacity 0) may pass no
+    // column arrays at all
     for (uint32_t c = 0; c < B.schema.n_payloads; ++c)
-        ol.col[c] = out_left[c];
+        ol.col[c] = out_left ? out_left[c] : nullptr;
     for (uint32_t c = 0; c < P.schema.n_payloads; ++c)
-        orr.col[c] = out_right[c];
+        orr.col[c] = out_right ? out_right[c] : nullptr;
 
     const unsigned fill_grid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(cap, kNaNT), (uint64_t)ctx->num_sms * 4));
-    k_na_clear<<<fill_grid, kNaNT, 0, ctx->stream>>>(s, cap);
-    PHJ_LAUNCHED(ctx, "noalloc_clear");
+    {
+        KTimer kt(ctx, "noalloc_clear", cap, cap * sizeof(Cell));
+        k_na_clear<<<fill_grid, kNaNT, 0, ctx->stream>>>(s, cap);
+        PHJ_LAUNCHED(ctx, "noalloc_clear");
+    }
     if (B.rows)
     {
+        KTimer kt(ctx, "noalloc_build", B.rows, B.rows * 8);
         k_na_build<<<(unsigned)std::min<uint64_t>(ceil_div(B.rows, kNaNT), (uint64_t)ctx->num_sms * 4), kNaNT, 0, ctx->stream>>>(bc.keys, B.rows,
                                                                                                                                  s, cap);
         PHJ_LAUNCHED(ctx, "noalloc_build");
     }
     if (P.rows)
     {
+        KTimer kt(ctx, "noalloc_probe", P.rows, P.rows * 8);
         const unsigned grid = (unsigned)std::min<uint64_t>(ceil_div(P.rows, kNaNT), (uint64_t)ctx->num_sms * 8);
         k_na_probe<<<grid, kNaNT, 0, ctx->stream>>>(pc, P.rows, bc, s, cap, ol, orr, out_cap);
         PHJ_LAUNCHED(ctx, "noalloc_probe");
@@ -206,6 +214,11 @@ extern "C" phj_status phj_run_chj_noalloc(phj_ctx * ctx, const phj_table * build
     if (out_rows)
         *out_rows = 0;
     phjg::DeviceScope dev(ctx);
+    if (!dev.ok())
+    {
+        ctx->last_error = dev.message(ctx);
+        return PHJ_ERR_CUDA;
+    }
     try
     {
         phjg::run_chj_noalloc(ctx, *build, *probe, out_capacity, out_keys, out_left, out_right, out_rows);

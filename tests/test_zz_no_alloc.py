@@ -1,6 +1,9 @@
 """The no-allocation join (phj_run_chj_noalloc) against the allocating CHJ
-entry point (phj_run_chj): the same rows, as sorted multisets, on two calls
-in a row (the second call must start from cleared scratch)."""
+entry point (phj_run_chj) and against the oracle (the CPU restatement of
+the reference's referenceOutput): the same rows, as sorted multisets, on
+two calls in a row (the second call must start from cleared scratch)."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -57,6 +60,7 @@ def test_no_alloc_matches_allocating_entry_point_twice(ctx, name):
     tb, tp = ctx.upload(b), ctx.upload(p)
     try:
         expected = allocating_rows(ctx, tb, tp)
+        assert O.compare_outputs(O.join_rows(b, p), expected) == ""
         for _ in range(2):
             got, n = noalloc_rows(ctx, tb, tp, b, p, len(expected) + 17)
             assert n == len(expected)
@@ -74,6 +78,7 @@ def test_no_alloc_largest_build_side(ctx):
     tb, tp = ctx.upload(b), ctx.upload(p)
     try:
         expected = allocating_rows(ctx, tb, tp)
+        assert O.compare_outputs(O.join_rows(b, p), expected) == ""
         for _ in range(2):
             got, n = noalloc_rows(ctx, tb, tp, b, p, len(expected))
             assert n == len(expected)
@@ -103,5 +108,21 @@ def test_no_alloc_rejects_oversized_build_and_reports_short_capacity(ctx):
         assert e.value.status == 7 and e.value.rows == len(expected)
         got, n = noalloc_rows(ctx, tb, tp, b, p, len(expected))
         assert O.compare_outputs(expected, got) == ""
+    finally:
+        tb.free(), tp.free()
+
+
+def test_no_alloc_counts_only_with_null_columns(ctx):
+    # capacity 0 and no column arrays at all: the call counts the rows,
+    # writes nothing and reports PHJ_ERR_CAPACITY with the count set
+    b, p = cases.make("c2_mini")
+    tb, tp = ctx.upload(b), ctx.upload(p)
+    try:
+        rows = C.c_uint64(0)
+        st = ctx.lib.phj_run_chj_noalloc(ctx.ptr, tb.handle, tp.handle, 0, None, None, None, C.byref(rows))
+        assert st == P.ERR_CAPACITY
+        assert rows.value == len(O.join_rows(b, p)) > 0
+        got, n = noalloc_rows(ctx, tb, tp, b, p, rows.value)
+        assert O.compare_outputs(O.join_rows(b, p), got) == ""
     finally:
         tb.free(), tp.free()
