@@ -12,10 +12,22 @@ import phj_gpu as P
 from golden import cases
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = "/root/reference/src"
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_SRC), reason="reference headers not on this machine")
+def reference_src():
+    """The reference's src/ directory: PHJ_REF_SRC, else the one the oracle's
+    recipe builds from; None (tests skip) where neither exists."""
+    d = os.environ.get("PHJ_REF_SRC")
+    if not d:
+        r = subprocess.run(["make", "-s", "--no-print-directory", "-C", os.path.join(ROOT, "oracle"), "ref-src"], capture_output=True, text=True)
+        d = r.stdout.strip() if r.returncode == 0 else ""
+    return d if d and os.path.isdir(d) else None
+
+
+REF_SRC = reference_src()
+
+
+@pytest.mark.skipif(REF_SRC is None, reason="reference headers not on this machine (set PHJ_REF_SRC)")
 def test_adapter_compiles_against_the_reference_types():
     subprocess.run(["g++", "-std=c++23", "-fsyntax-only", "-I", REF_SRC, "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "ref_types_check.cpp")], check=True)
