@@ -548,6 +548,27 @@ def main():
             out.free()
         line["chj"] = {"value": tuples / (statistics.mean(cms) / 1e3), "ms_per_step": statistics.mean(cms),
                        "fingerprint_equals_phj_pure": fp_chj == fp_main}
+        # the unpartitioned probe in sweeps over groups of sub-tables small
+        # enough for L2 (cells ~48 B a build row at the reference's load)
+        l2 = ctx.get_int("l2_bytes")
+        windows = 2
+        while windows < 256 and B * 48 // windows > l2 // 2:
+            windows *= 2
+        ctx.set_int("chj_windows", windows)
+        try:
+            out, _ = ctx.run_chj(b, p)
+            out.free()
+            wms = []
+            for _ in range(3):
+                ctx.flush_l2()
+                out, cres = ctx.run_chj(b, p)
+                wms.append(cres.e2e_wall_ms)
+                fp_w = out.fingerprint()
+                out.free()
+        finally:
+            ctx.set_int("chj_windows", 0)
+        line["chj_windowed"] = {"windows": windows, "value": tuples / (statistics.mean(wms) / 1e3), "ms_per_step": statistics.mean(wms),
+                                "fingerprint_equals_phj_pure": fp_w == fp_main}
 
     hb = hp = None
     if not (args.no_e2e and (args.no_cpu or rank != 0 or world != 1)):

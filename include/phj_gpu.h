@@ -169,6 +169,11 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        row) for CHJ and PHJ-PURE joins without repeated build keys whose
  *        2+ build payload columns fit 16 bytes, so the projection gathers one
  *        value per output row; 0 gathers column by column;
+ *   "chj_windows": CHJ probes in this many sweeps over the probe side
+ *        (a power of two up to 256), each looking up only the keys of one
+ *        group of consecutive top-8-bit sub-tables, so the tables a sweep
+ *        touches can stay in L2; 0 or 1 (default): one sweep.  Same output
+ *        rows, in another order;
  *   "probe_pass_bits": bits of the radix pass written out for the probe
  *        side, 1..11; 0 (default): PHJ-PURE chooses them from the build
  *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's

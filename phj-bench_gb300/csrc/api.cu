@@ -437,6 +437,58 @@ phj_output * probe_into_output(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, 
 {
     return probe_join(ctx, s, a, left, right);
 }
+
+// CHJ probe in windows of sub-tables (the "chj_windows" option): the 256
+// top-8-bit sub-tables are taken `windows` at a time in consecutive groups
+// (one contiguous region of cells each); a sweep over the whole probe side
+// looks up only the rows whose sub-table lies in the current group, so the
+// tables that sweep touches are that group's alone and can stay in L2 while
+// the probe keys stream past, then projects that sweep's matches after the
+// previous sweeps' rows.  Every sweep reads all the probe keys again, and
+// the build payloads are gathered in input order.  The output rows are
+// those of the one-sweep probe, in another order.
+phj_output * probe_chj_windows(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, const phj_schema & left, const phj_schema & right,
+                               uint32_t windows)
+{
+    ProbeArgs a = a_in;
+    if (a.any_dup && !a.row_cnt)
+        a.row_cnt = s.get<uint32_t>(std::max<uint64_t>(a.probe_rows, 1));
+    uint32_t * heads = s.get<uint32_t>(std::max<uint64_t>(a.probe_rows, 1));
+    uint32_t * counts = s.get<uint32_t>(probe_chunks(a.probe_rows) + 1);
+    const uint32_t n_sub = 1u << a.leaf_bits, step = std::max<uint32_t>(n_sub / windows, 1);
+    phj_output * o = nullptr;
+    uint64_t total = 0;
+    try
+    {
+        for (uint32_t lo = 0; lo < n_sub; lo += step)
+        {
+            a.win_lo = lo;
+            a.win_hi = lo + step;
+            Scratch sw(ctx);
+            const uint64_t rows = probe_lookup(ctx, sw, a, heads, counts);
+            if (!o)
+            {
+                // first window: the output sized for every window at its rate
+                const uint64_t est = (uint64_t)((double)rows * (double)(n_sub / step) * 1.0625) + 4096;
+                o = new_output(ctx, left, right, std::max(est, rows));
+            }
+            else if (total + rows > o->cap)
+                grow_output(ctx, o, std::max(o->cap * 2, total + rows), total);
+            probe_project(ctx, a, o, total, heads, counts, rows);
+            total += rows;
+        }
+        if (!o)
+            o = new_output(ctx, left, right, 0);
+        o->rows = total;
+    }
+    catch (...)
+    {
+        if (o)
+            free_output(ctx, o);
+        throw;
+    }
+    return o;
+}
 } // namespace
 
 // A bounded device wait that gave up leaves a code in the error word; the
@@ -499,7 +551,8 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     a.any_dup = lt.any_dup;
     a.uniform_log2cap = -1;
     pack_build_payloads(ctx, s, a, B.rows);
-    phj_output * o = probe_into_output(ctx, s, a, B.schema, P.schema);
+    phj_output * o =
+        ctx->chj_windows > 1 ? probe_chj_windows(ctx, s, a, B.schema, P.schema, ctx->chj_windows) : probe_into_output(ctx, s, a, B.schema, P.schema);
     PHJ_CUDA(cudaEventRecord(e2, ctx->stream));
     PHJ_CUDA(cudaEventSynchronize(e2));
     check_device_error(ctx);
@@ -1554,6 +1607,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->p1_stages = (uint32_t)value;
     else if (std::strcmp(name, "pack_build") == 0 && (value == 0 || value == 1))
         ctx->pack_build = (int)value;
+    else if (std::strcmp(name, "chj_windows") == 0 && value >= 0 && value <= 256 && (value & (value - 1)) == 0)
+        ctx->chj_windows = (uint32_t)value;
     else if (std::strcmp(name, "probe_pass_bits") == 0 && value >= 0 && value <= 11)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
@@ -1585,6 +1640,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->p1_stages;
     else if (std::strcmp(name, "pack_build") == 0)
         *value = ctx->pack_build;
+    else if (std::strcmp(name, "chj_windows") == 0)
+        *value = ctx->chj_windows;
     else if (std::strcmp(name, "probe_pass_bits") == 0)
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)

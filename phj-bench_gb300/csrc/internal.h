@@ -107,6 +107,7 @@ struct phj_ctx
     uint32_t p1_tile_rows = 0;    // first radix pass: rows per staged tile (0: chosen per row width)
     uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
     int pack_build = 1;           // pack unique-key build payloads row-major for the projection (0: columns)
+    uint32_t chj_windows = 0;     // CHJ: probe in this many windows of sub-tables (0 or 1: one sweep)
     uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
@@ -287,6 +288,10 @@ struct ProbeArgs
     // column.  nullptr: columns only.
     const uint4 * packed;
     uint8_t packed_off[kMaxCols];
+    // CHJ windowed probe: only rows whose sub-table (top leaf_bits hash
+    // bits) lies in [win_lo, win_hi) are looked up; the others record no
+    // match.  win_hi == 0: no window.
+    uint32_t win_lo, win_hi;
 };
 // PHJ/BEP lazy leaf tables.  Per probe batch: the leaves the batch touches
 // are flagged (one eviction per leaf and batch), the touched leaves still

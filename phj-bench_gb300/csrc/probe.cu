@@ -144,8 +144,10 @@ __device__ __forceinline__ void columns_pass(const Cols & src, void * const * ds
 }
 
 // Lookups: per probe row its head build row (kNoMatch when the key is
-// absent), per warp chunk its number of output rows.
-template <int kMode, bool kDup>
+// absent), per warp chunk its number of output rows.  kWin (CHJ only):
+// rows outside the sub-table window [a.win_lo, a.win_hi) touch no table and
+// record no match.
+template <int kMode, bool kDup, bool kWin = false>
 __global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
                                                        uint32_t * __restrict__ counts)
 {
@@ -188,6 +190,8 @@ __global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant_
             for (int u = 0; u < 4; ++u)
             {
                 mv[u] = make_ulonglong2(0ull, 0ull);
+                if (kWin && (live >> (g + u) & 1u) && (uint32_t)(int_hash64(key[g + u]) >> shift) - a.win_lo >= a.win_hi - a.win_lo)
+                    continue; // outside the window: the directory entry stays empty (no table)
                 if (kMode != kLeafUniform && (live >> (g + u) & 1u))
                     mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
             }
@@ -696,6 +700,11 @@ static void launch_probe(phj_ctx * ctx, const ProbeArgs & a, const OutCols * o, 
                          const char * name, uint64_t bytes)
 {
     auto lk = k_probe_lookup<kMode, kDup>;
+    if constexpr (kMode == kChj)
+        if (a.win_hi != 0)
+            lk = k_probe_lookup<kMode, kDup, true>;
+    if (kMode != kChj && a.win_hi != 0)
+        throw Error(PHJ_ERR_CUDA, "internal: sub-table windows are a CHJ probe form");
     // projection: plain (no repeated keys), range (grouped leaves) or flat
     // (chains expanded first)
     const int proj = !kDup ? 0 : (kMode != kChj && a.grouped) ? 1 : 2;

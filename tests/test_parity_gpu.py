@@ -491,3 +491,23 @@ def test_host_buffer_failure_after_build_shuffle_leaves_context_usable(ctx, sche
             assert O.compare_outputs(expected, O.serialize_output(jo)) == ""
     finally:
         ctx.set_int("host_chunk_rows", 16 << 20)
+
+
+@pytest.mark.parametrize("windows", [2, 16, 256])
+def test_chj_sub_table_windows(ctx, windows):
+    """The windowed CHJ probe (one sweep per group of sub-tables) gives the
+    oracle's rows on unique keys, repeated keys on both sides and the edge
+    keys, with packed and column-wise build payloads."""
+    ctx.set_int("chj_windows", windows)
+    try:
+        for name in ("c2_mini", "c3_mini", "edge"):
+            b, p = cases.make(name)
+            jo, fp, _ = run(ctx, "chj", b, p)
+            check(b, p, jo, fp)
+        ctx.set_int("pack_build", 0)
+        b, p = cases.make("c2_mini")
+        jo, fp, _ = run(ctx, "chj", b, p)
+        check(b, p, jo, fp)
+    finally:
+        ctx.set_int("pack_build", 1)
+        ctx.set_int("chj_windows", 0)
