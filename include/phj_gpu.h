@@ -174,6 +174,13 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        group of consecutive top-8-bit sub-tables, so the tables a sweep
  *        touches can stay in L2; 0 or 1 (default): one sweep.  Same output
  *        rows, in another order;
+ *   "bep_engine": PHJ (BEP) form; 0 (default) the device budget engine: one
+ *        persistent grid whose CTA groups (one per SM) each hold a share of
+ *        bep_budget_mib, scatter their slice of the probe side into
+ *        first-pass chains, refine at the reference's water marks and
+ *        evict leaves round-robin (first pass 1..11 bits with at most 13
+ *        bits below it; other configurations take the batch form); 1
+ *        budget-sized probe batches;
  *   "probe_pass_bits": bits of the radix pass written out for the probe
  *        side, 1..11; 0 (default): PHJ-PURE chooses them from the build
  *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's

@@ -980,6 +980,122 @@ static void run_phj_bep(phj_ctx * ctx, const phj_table & B, const phj_table & P,
     *out = o;
 }
 
+// PHJ (BEP) with the byte budget on the device (bep_engine.cu): the build
+// side is partitioned to full leaf depth (src/PHJBep.cpp:128-141) and its
+// tables only planned; one persistent grid then streams the probe side
+// through per-group unrefined chains, refines, evicts and builds leaves
+// lazily, and projects into the output.  The output is sized for one row
+// per probe row; a join with more output rows (repeated build keys) runs
+// the grid again into an output of the exact size the first run counted.
+static void run_phj_bep_engine(phj_ctx * ctx, const phj_table & B, const phj_table & P, const std::vector<uint32_t> & bits, uint64_t budget_mib,
+                               phj_output ** out, phj_bep_result * res)
+{
+    begin_run(ctx);
+    Scratch s(ctx);
+    uint32_t total_bits = 0;
+    for (uint32_t b : bits)
+        total_bits += b;
+    const uint32_t n_leaves = 1u << total_bits;
+    cudaEvent_t ev[4];
+    for (auto & e : ev)
+        e = take_event(ctx);
+    PHJ_CUDA(cudaEventRecord(ev[0], ctx->stream));
+    // -------- BUILD SHUFFLE, full leaf depth --------
+    const Cols bin = cols_of(B);
+    const Cols bpart = alloc_cols_like(s, B.schema, B.rows);
+    const Cols btmp = alloc_cols_like(s, B.schema, B.rows);
+    uint32_t * leaf_off = s.get<uint32_t>((uint64_t)n_leaves + 1);
+    radix_partition(ctx, s, bin, B.rows, bits, bpart, btmp, leaf_off, "build_scatter");
+    PHJ_CUDA(cudaEventRecord(ev[1], ctx->stream));
+    // -------- BUILD: table layout only; each table is built on first use --------
+    LeafTables lt;
+    lt.next = s.get<uint64_t>(std::max<uint64_t>(B.rows, 1));
+    build_leaf_tables(ctx, s, bpart, leaf_off, n_leaves, lt, true);
+    if (ctx->test_stuck_leaf >= 0 && (uint64_t)ctx->test_stuck_leaf < n_leaves)
+    {
+        const uint32_t building = 1;
+        PHJ_CUDA(cudaMemcpyAsync(lt.state + ctx->test_stuck_leaf, &building, sizeof(building), cudaMemcpyHostToDevice, ctx->stream));
+        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    PHJ_CUDA(cudaEventRecord(ev[2], ctx->stream));
+    // -------- PROBE: the device budget engine --------
+    BepEngineInput in{};
+    in.probe = cols_of(P);
+    in.probe_rows = P.rows;
+    in.build = bpart;
+    in.lt = &lt;
+    in.leaf_off = leaf_off;
+    in.b1 = bits[0];
+    in.total_bits = total_bits;
+    in.budget_bytes = budget_mib << 20;
+    phj_output * o = new_output(ctx, B.schema, P.schema, P.rows);
+    BepEngineResult r{};
+    try
+    {
+        if (P.rows > 0)
+        {
+            r = bep_engine_run(ctx, s, in, o);
+            if (r.err == 0 && r.out_rows > o->cap)
+            {
+                // repeated build keys: more output rows than probe rows
+                free_output(ctx, o);
+                o = nullptr;
+                o = new_output(ctx, B.schema, P.schema, r.out_rows);
+                Scratch s2(ctx);
+                const uint64_t built = r.tables_built;
+                r = bep_engine_run(ctx, s2, in, o);
+                r.tables_built += built;
+            }
+            if (r.err != 0)
+            {
+                PHJ_CUDA(cudaMemsetAsync(ctx->d_err, 0, sizeof(int), ctx->stream));
+                PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+                char buf[128];
+                if (r.err == 6 || r.err == 7)
+                {
+                    std::snprintf(buf, sizeof(buf), "PHJ (BEP): the device budget engine ran out of probe blocks (code %d)", r.err);
+                    throw Error(PHJ_ERR_CAPACITY, buf);
+                }
+                std::snprintf(buf, sizeof(buf), "a bounded device wait gave up (code %d)", r.err);
+                throw Error(PHJ_ERR_DEVICE_TIMEOUT, buf);
+            }
+        }
+        o->rows = r.out_rows;
+        PHJ_CUDA(cudaEventRecord(ev[3], ctx->stream));
+        PHJ_CUDA(cudaEventSynchronize(ev[3]));
+        debug_timeline(ctx, ev[0]);
+    }
+    catch (...)
+    {
+        if (o)
+            free_output(ctx, o);
+        throw;
+    }
+    if (std::getenv("PHJ_DEBUG"))
+        std::fprintf(stderr,
+                     "[phj] bep_engine: %u groups, %llu evict phases, %llu evictions, %llu refinements, peak %.3f GB of %.3f GB budget, pool %.2f GB, "
+                     "S %.3f ms E %.3f ms probe %.3f ms\n",
+                     r.groups, (unsigned long long)r.evict_phases, (unsigned long long)r.evictions, (unsigned long long)r.refinements,
+                     r.peak_bytes / 1e9, (double)(budget_mib << 20) / 1e9, r.pool_bytes / 1e9, r.ms_shuffle, r.ms_evict, r.ms_probe);
+    if (res)
+    {
+        const float bs = event_ms(ev[0], ev[1]), plan = event_ms(ev[1], ev[2]), e2e = event_ms(ev[0], ev[3]);
+        fill_phase(res->build_shuffle, bs, B.rows);
+        fill_phase(res->build, plan, B.rows); // the lazy builds count as eviction overhead
+        fill_phase(res->probe_shuffle, (float)r.ms_shuffle, P.rows);
+        fill_phase(res->probe, (float)r.ms_probe, P.rows);
+        fill_phase(res->eviction_overhead, std::max(0.f, e2e - bs - plan - (float)r.ms_shuffle - (float)r.ms_probe), P.rows);
+        res->e2e_wall_ms = e2e;
+        res->peak_mem_bytes = ctx->peak_bytes;
+        res->bep_budget_mib = budget_mib;
+        res->bep_evictions = r.evictions;
+        res->bep_refinements = r.refinements;
+        res->bep_peak_bytes = r.peak_bytes;
+        res->bep_build_skip_retries = r.skip_retries;
+    }
+    *out = o;
+}
+
 // On every exit from a host-buffer join, errors included, waits for the
 // copies still queued on the h2d and d2h streams, so that no buffer the
 // table guard or the scratch hands back to the pool (both free in the
@@ -1609,6 +1725,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->pack_build = (int)value;
     else if (std::strcmp(name, "chj_windows") == 0 && value >= 0 && value <= 256 && (value & (value - 1)) == 0)
         ctx->chj_windows = (uint32_t)value;
+    else if (std::strcmp(name, "bep_engine") == 0 && (value == 0 || value == 1))
+        ctx->bep_engine = (int)value;
     else if (std::strcmp(name, "probe_pass_bits") == 0 && value >= 0 && value <= 11)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
@@ -1642,6 +1760,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->pack_build;
     else if (std::strcmp(name, "chj_windows") == 0)
         *value = ctx->chj_windows;
+    else if (std::strcmp(name, "bep_engine") == 0)
+        *value = ctx->bep_engine;
     else if (std::strcmp(name, "probe_pass_bits") == 0)
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
@@ -1939,7 +2059,10 @@ phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_tab
             total += b;
         if (total > 20)
             throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) on the device takes at most 20 radix bits (2^20 leaves)");
-        run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
+        if (ctx->bep_engine == 0 && bep_engine_supported(bits[0], total))
+            run_phj_bep_engine(ctx, *build, *probe, bits, bep_budget_mib, out, result);
+        else
+            run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
     });
 }
 

@@ -108,6 +108,7 @@ struct phj_ctx
     uint32_t p1_stages = 0;       // first radix pass: depth of the bulk-copy ring (0: chosen per row width)
     int pack_build = 1;           // pack unique-key build payloads row-major for the projection (0: columns)
     uint32_t chj_windows = 0;     // CHJ: probe in this many windows of sub-tables (0 or 1: one sweep)
+    int bep_engine = 0;           // PHJ/BEP: 0 the device budget engine, 1 budget-sized probe batches
     uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
@@ -323,6 +324,34 @@ struct BepLeaves
 // (ctx->leaf_mark) before this runs.
 bool bep_build_touched(phj_ctx * ctx, const BepLeaves & b);
 void set_bep_smem_limits(int smem_optin);
+
+// ----- bep_engine.cu ------------------------------------------------------------------
+// PHJ/BEP with the probe-side byte budget kept on the device: one
+// persistent grid of CTA groups with per-group unrefined chains, water
+// marks, refinement, round-robin eviction and lazy leaf builds.
+struct BepEngineInput
+{
+    Cols probe; // probe side in input order
+    uint64_t probe_rows;
+    Cols build; // leaf-partitioned build side (keys and payloads)
+    const LeafTables * lt; // lazily built tables (lt->state set)
+    const uint32_t * leaf_off;
+    uint32_t b1, total_bits;
+    uint64_t budget_bytes; // the whole run's budget (bep_budget_mib)
+};
+struct BepEngineResult
+{
+    int err;           // device error code (0: none)
+    uint64_t out_rows; // output rows of the join (may exceed the output's capacity)
+    uint64_t evictions, refinements, skip_retries, tables_built, evict_phases, peak_bytes, pool_bytes;
+    double ms_shuffle, ms_evict, ms_probe; // one group's time in scatter/refine, eviction bookkeeping and probing
+    uint32_t groups;
+};
+// Whether the engine takes this radix configuration (first pass 1..11 bits,
+// at most 13 bits below it).
+bool bep_engine_supported(uint32_t b1, uint32_t total_bits);
+// One engine run into `out` (rows past out->cap are counted, not written).
+BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput & in, phj_output * out);
 
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);

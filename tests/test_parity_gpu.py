@@ -157,10 +157,15 @@ def test_bep_radix_configs(ctx, bits):
 
 @pytest.mark.parametrize("budget", [1, 2, 64])
 def test_bep_budget_batches_and_counters(ctx, budget):
-    # 600K probe rows of 12 bytes (7.2 MB): a 1 MiB budget gives 8 batches.
+    # The batch form ("bep_engine" 1): 600K probe rows of 12 bytes (7.2 MB);
+    # a 1 MiB budget gives 8 batches.
     b, p = bep_inputs(50000, 600000, 101)
     bits = [3, 5]
-    jo, fp, res = run(ctx, "phj", b, p, bits, budget_mib=budget)
+    ctx.set_int("bep_engine", 1)
+    try:
+        jo, fp, res = run(ctx, "phj", b, p, bits, budget_mib=budget)
+    finally:
+        ctx.set_int("bep_engine", 0)
     check(b, p, jo, fp)
     row_bytes = 8 + 4
     batch_rows = min(600000, max(4096, ((budget << 20) // row_bytes) & ~255))
@@ -189,9 +194,63 @@ def test_bep_small_batches_multi_match(ctx):
     pk = G.gen_keys(4, 300000, 133, 16, domain=used, match_permille=500)
     b = P.BlockStream([P.U16, P.U128], bk, G.payload_columns(134, [P.U16, P.U128], 16000))
     p = P.BlockStream([P.U128], pk, G.payload_columns(135, [P.U128], 300000))
-    jo, fp, res = run(ctx, "phj", b, p, [2, 4], budget_mib=1)
+    ctx.set_int("bep_engine", 1)
+    try:
+        jo, fp, res = run(ctx, "phj", b, p, [2, 4], budget_mib=1)
+    finally:
+        ctx.set_int("bep_engine", 0)
     check(b, p, jo, fp)
     assert res.bep_peak_bytes == (((1 << 20) // 24) & ~255) * 24
+    # the device budget engine on the same inputs
+    jo, fp, res = run(ctx, "phj", b, p, [2, 4], budget_mib=1)
+    check(b, p, jo, fp)
+    assert res.bep_evictions > 64 and res.bep_refinements >= 4
+
+
+@pytest.mark.parametrize("budget", [1, 2, 64])
+def test_bep_device_budget_counters(ctx, budget):
+    """The device budget engine (default): 600K probe rows of 12 bytes
+    (7.2 MB) through per-group unrefined chains.  At 64 MiB the leaf high
+    water (40 MiB) is never reached: every row is refined before any
+    eviction, the peak is the whole probe side and each of the 256 leaves
+    is evicted once, in the final drain.  At 1-2 MiB the high water is
+    crossed mid-stream: leaves are evicted more than once and the peak stays
+    near the budget."""
+    b, p = bep_inputs(50000, 600000, 101)
+    bits = [3, 5]
+    jo, fp, res = run(ctx, "phj", b, p, bits, budget_mib=budget)
+    check(b, p, jo, fp)
+    row_bytes = 12
+    groups = ctx.get_int("num_sms")
+    assert res.bep_refinements >= 8
+    if budget == 64:
+        assert res.bep_peak_bytes == 600000 * row_bytes
+        assert res.bep_evictions == 256
+    else:
+        assert res.bep_evictions > 256
+        # the leaf high water (5/8 of the budget) plus one wave of refines,
+        # each group's at most half its share plus a tile of 256 rows
+        wave = groups * ((budget << 20) // groups // 2 + 256 * row_bytes)
+        assert (budget << 20) * 5 // 8 <= res.bep_peak_bytes <= (budget << 20) * 5 // 8 + wave
+    assert res.bep_build_skip_retries == 0
+    assert res.probe.wall_ms > 0 and res.e2e_wall_ms >= res.probe.wall_ms
+
+
+@pytest.mark.parametrize("bits", [[2, 4], [6, 6, 6], [8], [1, 12]])
+def test_bep_engine_and_batches_agree(ctx, bits):
+    """Both PHJ (BEP) forms give the oracle's rows, on unique keys with a
+    tight budget (evictions mid-stream) and on repeated build keys (more
+    output rows than probe rows: the engine runs again into an output of
+    the exact size)."""
+    for name in ("c3_mini", "c4_mini", "c2_mini"):
+        b, p = cases.make(name)
+        for engine in (0, 1):
+            ctx.set_int("bep_engine", engine)
+            try:
+                jo, fp, _ = run(ctx, "phj", b, p, bits, budget_mib=1)
+            finally:
+                ctx.set_int("bep_engine", 0)
+            check(b, p, jo, fp)
 
 
 def test_bep_repeated_runs_identical(ctx):
