@@ -62,7 +62,6 @@ namespace
 constexpr int kENT = 1024; // threads of a group's CTA
 constexpr uint32_t kNone = 0xFFFFFFFFu;
 constexpr uint32_t kNotBuilt = 0, kBuilding = 1, kBuilt = 2, kBuiltDup = 3;
-constexpr uint32_t kRowsPerThread = 4; // E probe: rows a thread looks up per step
 
 // error codes written to the context's error word
 constexpr int kErrWait = 4;    // a BUILDING leaf was not published in time
@@ -83,8 +82,9 @@ struct EngineCtl
     unsigned long long ev_len;
     unsigned long long out_rows; // output rows placed (the exact total, also past capacity)
     long long free_top;          // blocks on the free stack
-    unsigned int work_n, work_next;
+    unsigned int work_n;
     unsigned int build_n, build_next;
+    unsigned long long work_next;
     unsigned long long evictions, refinements, skip_retries, tables_built, evict_phases;
     unsigned long long ns_shuffle, ns_evict, ns_probe; // group 0's time in S, E bookkeeping, E probing
     unsigned long long rows_scattered, rows_refined, rows_probed, rows_claimed; // row totals per step (checks)
@@ -121,6 +121,7 @@ struct EngineArgs
     uint32_t * blk_state; // refined and holding unprobed rows: its bucket; otherwise kNone
     uint32_t * blk_rows;
     uint32_t * blk_rem;
+    uint32_t * blk_bucket; // the bucket of a refined block (kept after the block is freed)
     uint32_t * blk_lfirst; // leaf-in-bucket of a refined block's first and last row
     uint32_t * blk_llast;
     // the eviction cursor when the block was refined: the block's rows of
@@ -297,12 +298,14 @@ struct Smem
 {
     uint8_t * stage;  // page rows in the block layout; the leaf builds' cells
     uint16_t * perm;  // page entries
+    uint16_t * src;   // page entries: the stage row of each sorted position
     uint32_t * bins;  // max(buckets, leaves per bucket, page) entries
     uint32_t * boff;  // buckets: scatter offsets
     uint32_t * nbpre; // buckets: new blocks per bucket, then their prefix
     uint32_t * fill;  // buckets: rows in each chain's last block (page: no block)
     uint32_t * clen;  // buckets: blocks in each chain
     uint32_t * urows; // buckets: unrefined rows per bucket
+    uint32_t * acc;   // leaves per bucket: rows a refine adds to each leaf
     uint32_t * ws;    // scan scratch (kENT / 32 words)
     uint32_t * scal;  // scalars (32 words, 8-byte aligned)
 };
@@ -313,32 +316,50 @@ struct Smem
 constexpr int kTileDone = 0, kTileNoRoom = 1, kTileFailed = 2;
 
 // Returns kTileDone, kTileNoRoom (too few free blocks: nothing done) or
-// kTileFailed (the grid is ending).
+// kTileFailed (the grid is ending).  sm.bins[0, buckets) is zero on entry
+// and on a kTileDone return.
 __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, uint64_t r0, uint32_t n)
 {
     const uint32_t page = 1u << a.page_log2;
     const uint32_t P1 = a.n_buckets;
-    for (uint32_t p = threadIdx.x; p < P1; p += kENT)
-        sm.bins[p] = 0;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += kENT)
+    // the tile into the stage in input order (one read of the input), and
+    // the first-pass bucket of every row
+    for (uint32_t i0 = 0; i0 < n; i0 += 4 * kENT)
     {
-        const uint32_t p = (uint32_t)(int_hash64(a.pin.keys[r0 + i]) >> (64u - a.b1));
-        sm.perm[i] = (uint16_t)p;
-        atomicAdd(&sm.bins[p], 1u);
+        uint64_t k[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = i0 + u * kENT + threadIdx.x;
+            k[u] = i < n ? a.pin.keys[r0 + i] : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = i0 + u * kENT + threadIdx.x;
+            if (i < n)
+            {
+                reinterpret_cast<uint64_t *>(sm.stage)[i] = k[u];
+                for (uint32_t c = 0; c < a.pin.n; ++c)
+                    copy_elem(sm.stage + a.col_off[c], i, a.pin.col[c], r0 + i, a.pin.width[c]);
+                const uint32_t p = (uint32_t)(int_hash64(k[u]) >> (64u - a.b1));
+                sm.perm[i] = (uint16_t)p;
+                atomicAdd(&sm.bins[p], 1u);
+            }
+        }
     }
     __syncthreads();
-    // offsets of each bucket's rows in the sorted tile, and the blocks each
-    // bucket's chain needs (an empty chain counts as a full last block)
+    // per bucket its rows (high half) and the blocks its chain needs (low
+    // half; an empty chain counts as a full last block), scanned at once
     for (uint32_t p = threadIdx.x; p < P1; p += kENT)
     {
         const uint32_t c = sm.bins[p];
-        sm.boff[p] = c;
-        sm.nbpre[p] = c == 0 ? 0u : (sm.fill[p] + c + page - 1) / page - 1u;
+        const uint32_t nb = c == 0 ? 0u : (sm.fill[p] + c + page - 1) / page - 1u;
+        sm.boff[p] = (c << 16) | nb;
     }
     __syncthreads();
-    scan_bins(sm.boff, P1, sm.ws);
-    const uint32_t nb_total = scan_bins(sm.nbpre, P1, sm.ws);
+    const uint32_t tot = scan_bins(sm.boff, P1, sm.ws);
+    const uint32_t nb_total = tot & 0xFFFFu;
     if (threadIdx.x == 0)
     {
         sm.scal[0] = 0;
@@ -367,11 +388,18 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
     }
     __syncthreads();
     if (sm.scal[0])
+    {
+        for (uint32_t p = threadIdx.x; p < P1; p += kENT)
+            sm.bins[p] = 0;
+        __syncthreads();
         return kTileNoRoom;
-    // new blocks onto the chains
+    }
+    // new blocks onto the chains; the cursors of the sorted tile
     for (uint32_t p = threadIdx.x; p < P1; p += kENT)
     {
-        const uint32_t nb = (p + 1 < P1 ? sm.nbpre[p + 1] : nb_total) - sm.nbpre[p];
+        const uint32_t off = sm.boff[p] >> 16, nb0 = sm.boff[p] & 0xFFFFu;
+        const uint32_t nb = ((p + 1 < P1 ? sm.boff[p + 1] : tot) & 0xFFFFu) - nb0;
+        sm.bins[p] = off;
         if (nb == 0)
             continue;
         const uint32_t len = sm.clen[p];
@@ -383,43 +411,39 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
         }
         uint32_t * ch = a.chain + ((uint64_t)g * P1 + p) * a.maxb;
         for (uint32_t j = 0; j < nb; ++j)
-            ch[len + j] = __ldcg(a.free_stack + sm.scal[1] + sm.nbpre[p] + j);
+            ch[len + j] = __ldcg(a.free_stack + sm.scal[1] + nb0 + j);
     }
-    // the rows, sorted by bucket, into the stage
-    for (uint32_t p = threadIdx.x; p < P1; p += kENT)
-        sm.bins[p] = sm.boff[p];
     __syncthreads();
     if (sm.scal[0])
         return kTileFailed;
+    // the stage row of every sorted position
     for (uint32_t i = threadIdx.x; i < n; i += kENT)
-    {
-        const uint32_t s = atomicAdd(&sm.bins[sm.perm[i]], 1u);
-        reinterpret_cast<uint64_t *>(sm.stage)[s] = a.pin.keys[r0 + i];
-        for (uint32_t c = 0; c < a.pin.n; ++c)
-            copy_elem(sm.stage + a.col_off[c], s, a.pin.col[c], r0 + i, a.pin.width[c]);
-    }
+        sm.src[atomicAdd(&sm.bins[sm.perm[i]], 1u)] = (uint16_t)i;
     __syncthreads();
-    // the sorted rows out to the chains' blocks: consecutive rows of a
-    // bucket go to consecutive rows of its blocks
+    // the rows out to the chains' blocks in sorted order: consecutive rows
+    // of a bucket go to consecutive rows of its blocks
     for (uint32_t s = threadIdx.x; s < n; s += kENT)
     {
-        const uint64_t key = reinterpret_cast<const uint64_t *>(sm.stage)[s];
+        const uint32_t r = sm.src[s];
+        const uint64_t key = reinterpret_cast<const uint64_t *>(sm.stage)[r];
         const uint32_t p = (uint32_t)(int_hash64(key) >> (64u - a.b1));
-        const uint32_t q = sm.fill[p] + (s - sm.boff[p]); // slot counted from the chain's last block
+        const uint32_t q = sm.fill[p] + (s - (sm.boff[p] >> 16)); // slot counted from the chain's last block
         const uint32_t idx = sm.clen[p] + (q >> a.page_log2) - 1u;
         const uint32_t blk = a.chain[((uint64_t)g * P1 + p) * a.maxb + idx];
-        copy_row<false>(a, block_ptr(a, blk), q & (page - 1), sm.stage, s);
+        copy_row<false>(a, block_ptr(a, blk), q & (page - 1), sm.stage, r);
     }
     __syncthreads();
     for (uint32_t p = threadIdx.x; p < P1; p += kENT)
     {
-        const uint32_t c = (p + 1 < P1 ? sm.boff[p + 1] : n) - sm.boff[p];
-        if (c == 0)
+        sm.bins[p] = 0;
+        const uint32_t c = (sm.boff[p + 1 < P1 ? p + 1 : p] >> 16) - (sm.boff[p] >> 16);
+        const uint32_t cnt = p + 1 < P1 ? c : n - (sm.boff[p] >> 16);
+        if (cnt == 0)
             continue;
-        const uint32_t nb = (p + 1 < P1 ? sm.nbpre[p + 1] : nb_total) - sm.nbpre[p];
-        sm.fill[p] = ((sm.fill[p] + c - 1) & (page - 1)) + 1;
+        const uint32_t nb = ((p + 1 < P1 ? sm.boff[p + 1] : tot) & 0xFFFFu) - (sm.boff[p] & 0xFFFFu);
+        sm.fill[p] = ((sm.fill[p] + cnt - 1) & (page - 1)) + 1;
         sm.clen[p] += nb;
-        sm.urows[p] += c;
+        sm.urows[p] += cnt;
     }
     __syncthreads();
     return kTileDone;
@@ -436,6 +460,9 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
     const uint32_t len = sm.clen[p], rows = sm.urows[p];
     const uint32_t * ch = a.chain + ((uint64_t)g * a.n_buckets + p) * a.maxb;
     const uint32_t shift = 64u - a.total_bits;
+    // the rows each leaf gains, summed over the bucket's blocks
+    for (uint32_t l = threadIdx.x; l < LB; l += kENT)
+        sm.acc[l] = 0;
     for (uint32_t j = 0; j < len; ++j)
     {
         const uint32_t blk = ch[j];
@@ -444,31 +471,45 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
         for (uint32_t l = threadIdx.x; l < LB; l += kENT)
             sm.bins[l] = 0;
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < n; i += kENT)
+        for (uint32_t i0 = 0; i0 < n; i0 += 4 * kENT)
         {
-            copy_row<true>(a, sm.stage, i, B, i);
-            const uint32_t l = (uint32_t)(int_hash64(reinterpret_cast<const uint64_t *>(sm.stage)[i]) >> shift) & (LB - 1u);
-            sm.perm[i] = (uint16_t)l;
-            atomicAdd(&sm.bins[l], 1u);
+            uint64_t k[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                const uint32_t i = i0 + u * kENT + threadIdx.x;
+                k[u] = i < n ? __ldcg(reinterpret_cast<const unsigned long long *>(B) + i) : 0ull;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+            {
+                const uint32_t i = i0 + u * kENT + threadIdx.x;
+                if (i < n)
+                {
+                    reinterpret_cast<uint64_t *>(sm.stage)[i] = k[u];
+                    for (uint32_t c = 0; c < a.pin.n; ++c)
+                        copy_elem_cg(sm.stage + a.col_off[c], i, B + a.col_off[c], i, a.pin.width[c]);
+                    const uint32_t l = (uint32_t)(int_hash64(k[u]) >> shift) & (LB - 1u);
+                    sm.perm[i] = (uint16_t)l;
+                    atomicAdd(&sm.bins[l], 1u);
+                }
+            }
         }
         __syncthreads();
-        // the rows each leaf gains, then each leaf's first sorted position
         for (uint32_t l = threadIdx.x; l < LB; l += kENT)
-            if (sm.bins[l])
-                atomicAdd(a.leaf_rows + ((uint64_t)p << a.lb_log2) + l, sm.bins[l]);
-        __syncthreads();
+            sm.acc[l] += sm.bins[l];
         scan_bins(sm.bins, LB, sm.ws);
         // every row's sorted position (a row's order within its leaf does
-        // not matter) ...
+        // not matter), inverted into the source row of every position
+        // (bins reused: page entries), then the block written back in
+        // sorted order with consecutive stores
         for (uint32_t i = threadIdx.x; i < n; i += kENT)
             sm.perm[i] = (uint16_t)atomicAdd(&sm.bins[sm.perm[i]], 1u);
         __syncthreads();
-        // ... inverted into the source row of every position (bins reused) ...
         uint32_t * src = sm.bins;
         for (uint32_t i = threadIdx.x; i < n; i += kENT)
             src[sm.perm[i]] = i;
         __syncthreads();
-        // ... and the block written back in sorted order, consecutive stores
         for (uint32_t s = threadIdx.x; s < n; s += kENT)
             copy_row<false>(a, B, s, sm.stage, src[s]);
         if (threadIdx.x == 0)
@@ -479,11 +520,15 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
             a.blk_llast[blk] = (uint32_t)(int_hash64(reinterpret_cast<const uint64_t *>(sm.stage)[src[n - 1]]) >> shift) & (LB - 1u);
             a.blk_rows[blk] = n;
             a.blk_rem[blk] = n;
+            a.blk_bucket[blk] = p;
             a.blk_c0[blk] = vload(&a.ctl->cursor); // the cursor stands still outside E
             a.blk_state[blk] = p;
         }
         __syncthreads();
     }
+    for (uint32_t l = threadIdx.x; l < LB; l += kENT)
+        if (sm.acc[l])
+            atomicAdd(a.leaf_rows + ((uint64_t)p << a.lb_log2) + l, sm.acc[l]);
     if (threadIdx.x == 0)
     {
         atomicAdd(&a.ctl->global_leaf_rows, (unsigned long long)rows);
@@ -555,18 +600,35 @@ __device__ void evict_range(const EngineArgs & a, const Smem & sm, bool final_dr
         const uint64_t need = g_rows > keep_max ? g_rows - keep_max : 0;
         uint64_t taken = 0;
         len = 0;
-        for (uint64_t base = 0; base < n && taken < need; base += kENT)
+        constexpr uint32_t kPer = 8; // leaves a thread sums per step
+        for (uint64_t base = 0; base < n && taken < need; base += (uint64_t)kENT * kPer)
         {
-            const uint64_t i = base + threadIdx.x;
-            const uint32_t v = i < n ? __ldcg(a.leaf_rows + (lo + i) % n) : 0u;
+            const uint64_t i0 = base + (uint64_t)threadIdx.x * kPer;
+            uint32_t v[kPer], mine = 0;
+#pragma unroll
+            for (uint32_t u = 0; u < kPer; ++u)
+            {
+                v[u] = i0 + u < n ? __ldcg(a.leaf_rows + (lo + i0 + u) % n) : 0u;
+                mine += v[u];
+            }
             uint32_t tot;
-            const uint32_t ex = block_excl_scan<kENT>(v, sm.ws, &tot);
+            const uint32_t ex = block_excl_scan<kENT>(mine, sm.ws, &tot);
             if (threadIdx.x == 0)
                 sm.scal[6] = kNone;
             __syncthreads();
             // the leaf whose inclusive prefix first reaches `need`
-            if (i < n && taken + ex < need && taken + ex + v >= need)
-                sm.scal[6] = threadIdx.x;
+            if (taken + ex < need && taken + ex + mine >= need)
+            {
+                uint64_t run = taken + ex;
+                uint32_t u = 0;
+                for (; u < kPer; ++u)
+                {
+                    run += v[u];
+                    if (run >= need)
+                        break;
+                }
+                sm.scal[6] = threadIdx.x * kPer + u;
+            }
             __syncthreads();
             const uint32_t hit = sm.scal[6];
             __syncthreads();
@@ -578,7 +640,7 @@ __device__ void evict_range(const EngineArgs & a, const Smem & sm, bool final_dr
             else
             {
                 taken += tot;
-                len = umin64(base + kENT, n);
+                len = umin64(base + (uint64_t)kENT * kPer, n);
             }
         }
     }
@@ -642,58 +704,50 @@ __device__ __forceinline__ uint64_t block_len(const EngineArgs & a, unsigned lon
     return end <= lo_abs ? 0 : umin64(len, end - lo_abs);
 }
 
-// Builds the table of leaf L (this group won NOT_BUILT -> BUILDING): in
-// shared memory when it fits, else in place; threads the next-chain.
-// Returns whether a key repeats.
-__device__ bool build_leaf(const EngineArgs & a, const Smem & sm, uint32_t L)
+// Builds the table of leaf L in place (this warp won NOT_BUILT ->
+// BUILDING) and threads the next-chain.  Returns whether a key repeats.
+__device__ bool build_leaf_warp(const EngineArgs & a, uint32_t L, uint32_t lane)
 {
-    const LeafMeta m = a.meta[L];
+    const LeafMeta m = a.meta[L]; // its place and size are planned before the launch
     bool dup = false;
     if (m.has_table)
     {
         const uint64_t cap = 1ull << m.log2cap;
-        const bool in_smem = cap <= a.smem_cells;
-        Cell * tab = in_smem ? reinterpret_cast<Cell *>(sm.stage) : a.cells + m.table_off;
-        for (uint64_t j = threadIdx.x; j < cap; j += kENT)
+        Cell * tab = a.cells + m.table_off;
+        for (uint64_t j = lane; j < cap; j += 32)
             reinterpret_cast<ulonglong2 *>(tab)[j] = make_ulonglong2(0ull, INVALID_REF);
-        __syncthreads();
+        __syncwarp();
         const uint32_t r0 = m.row_off, r1 = a.leaf_off[L + 1];
-        for (uint32_t r = r0 + threadIdx.x; r < r1; r += kENT)
+        for (uint32_t r = r0 + lane; r < r1; r += 32)
         {
             const uint64_t k = a.bpart.keys[r];
-            const uint64_t h = int_hash64(k);
-            const uint64_t prev = in_smem ? table_insert<true>(tab, cap, h, k, make_ref(0, r)) : table_insert<false>(tab, cap, h, k, make_ref(0, r));
+            const uint64_t prev = table_insert<false>(tab, cap, int_hash64(k), k, make_ref(0, r));
             a.next[r] = prev;
             dup |= ref_valid(prev);
         }
-        dup = __syncthreads_or(dup);
-        if (in_smem)
-            for (uint64_t j = threadIdx.x; j < cap; j += kENT)
-                reinterpret_cast<ulonglong2 *>(a.cells + m.table_off)[j] = reinterpret_cast<const ulonglong2 *>(tab)[j];
     }
-    __syncthreads();
-    return dup;
+    return __any_sync(0xffffffffu, dup);
 }
 
-// E1b: the claimed leaves still NOT_BUILT, taken from the queue one at a
-// time per group.  False when a wait on a BUILDING leaf ran out.
-__device__ bool build_claimed(const EngineArgs & a, const Smem & sm)
+// E1b: every warp takes claimed leaves from the queue and builds those it
+// wins NOT_BUILT -> BUILDING for; a leaf another warp is building is waited
+// for, bounded (the grid then ends with kErrWait).
+__device__ void build_claimed(const EngineArgs & a)
 {
+    const uint32_t lane = threadIdx.x & 31;
     for (;;)
     {
-        if (threadIdx.x == 0)
+        uint32_t L = kNone, won = 0;
+        if (lane == 0)
         {
             const uint32_t i = atomicAdd(&a.ctl->build_next, 1u);
-            sm.scal[8] = i < vload(&a.ctl->build_n) ? __ldcg(a.build_queue + i) : kNone;
-            sm.scal[9] = 0;
-            if (sm.scal[8] != kNone)
+            L = i < vload(&a.ctl->build_n) ? __ldcg(a.build_queue + i) : kNone;
+            if (L != kNone)
             {
-                const uint32_t L = sm.scal[8];
                 if (atomicCAS(a.state + L, kNotBuilt, kBuilding) == kNotBuilt)
-                    sm.scal[9] = 1; // won: this group builds it
+                    won = 1;
                 else if (ld_acquire_u32(a.state + L) < kBuilt)
                 {
-                    // another group is building it: wait, bounded
                     atomicAdd(&a.ctl->skip_retries, 1ull);
                     const uint64_t t0 = now_ns();
                     uint32_t spins = 0;
@@ -711,16 +765,14 @@ __device__ bool build_claimed(const EngineArgs & a, const Smem & sm)
                 }
             }
         }
-        __syncthreads();
-        const uint32_t L = sm.scal[8];
-        const bool won = sm.scal[9] != 0;
-        __syncthreads();
+        L = __shfl_sync(0xffffffffu, L, 0);
+        won = __shfl_sync(0xffffffffu, won, 0);
         if (L == kNone || aborted(a))
-            return !aborted(a);
+            return;
         if (won)
         {
-            const bool dup = build_leaf(a, sm, L);
-            if (threadIdx.x == 0)
+            const bool dup = build_leaf_warp(a, L, lane);
+            if (lane == 0)
             {
                 a.meta[L].dup = dup ? 1 : 0;
                 __threadfence();
@@ -728,39 +780,30 @@ __device__ bool build_claimed(const EngineArgs & a, const Smem & sm)
                 atomicAdd(&a.ctl->tables_built, 1ull);
             }
         }
-        __syncthreads();
     }
 }
 
-// Rows of the leaf-sorted block B (rows [0, n)) whose leaf-in-bucket is
-// below l0 and below l1, i.e. the bounds of its rows of leaves [l0, l1);
-// counted by the whole CTA into scal[12] and scal[13].
-__device__ void leaf_bounds(const EngineArgs & a, const Smem & sm, const uint8_t * B, uint32_t n, uint32_t l0, uint32_t l1)
+// First row of the leaf-sorted block B (rows [lo, hi)) whose leaf-in-bucket
+// is >= l: a 32-way search by one warp.
+__device__ uint32_t lower_bound_warp(const EngineArgs & a, const uint8_t * B, uint32_t lo, uint32_t hi, uint32_t l, uint32_t lane)
 {
-    if (threadIdx.x == 0)
-        sm.scal[12] = sm.scal[13] = 0;
-    __syncthreads();
-    uint32_t c0 = 0, c1 = 0;
     const uint32_t mask = (1u << a.lb_log2) - 1u, shift = 64u - a.total_bits;
-    for (uint32_t i = threadIdx.x; i < n; i += kENT)
+    const unsigned long long * keys = reinterpret_cast<const unsigned long long *>(B);
+    while (hi - lo > 32)
     {
-        const uint32_t l = (uint32_t)(int_hash64(__ldcg(reinterpret_cast<const unsigned long long *>(B) + i)) >> shift) & mask;
-        c0 += l < l0;
-        c1 += l < l1;
+        const uint32_t step = (hi - lo + 31) / 32;
+        const uint32_t x = lo + lane * step;
+        const bool below = x < hi && ((uint32_t)(int_hash64(__ldcg(keys + x)) >> shift) & mask) < l;
+        const uint32_t c = __popc(__ballot_sync(0xffffffffu, below));
+        // rows before lo are below l, rows from hi on are not
+        const uint32_t nlo = c ? lo + (c - 1) * step + 1 : lo;
+        const uint32_t nhi = c < 32 && lo + c * step < hi ? lo + c * step : hi;
+        lo = nlo;
+        hi = nhi;
     }
-    for (int o = 16; o > 0; o >>= 1)
-    {
-        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
-        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
-    }
-    if ((threadIdx.x & 31) == 0)
-    {
-        if (c0)
-            atomicAdd(&sm.scal[12], c0);
-        if (c1)
-            atomicAdd(&sm.scal[13], c1);
-    }
-    __syncthreads();
+    const uint32_t x = lo + lane;
+    const bool below = x < hi && ((uint32_t)(int_hash64(__ldcg(keys + x)) >> shift) & mask) < l;
+    return lo + __popc(__ballot_sync(0xffffffffu, below));
 }
 
 // Match count and head build row of one probe key.  The leaf's table was
@@ -784,6 +827,7 @@ __device__ __forceinline__ uint32_t lookup(const EngineArgs & a, uint64_t key, u
         cap = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
         tab = a.cells + m.x;
     }
+    const uint32_t st = __ldcg(a.state + L); // beside the first cell load
     const uint64_t mask = cap - 1;
     uint64_t pos = probe_start(h, cap), r = INVALID_REF;
     for (uint64_t step = 0; step < cap; ++step)
@@ -801,7 +845,7 @@ __device__ __forceinline__ uint32_t lookup(const EngineArgs & a, uint64_t key, u
     if (!ref_valid(r))
         return 0;
     head = ref_row(r);
-    if (__ldcg(a.state + L) != kBuiltDup)
+    if (st != kBuiltDup)
         return 1;
     uint32_t c = 1;
     for (unsigned long long x = __ldcg(reinterpret_cast<const unsigned long long *>(a.next) + head); ref_valid(x);
@@ -810,46 +854,60 @@ __device__ __forceinline__ uint32_t lookup(const EngineArgs & a, uint64_t key, u
     return c;
 }
 
-// E2: probe rows [r0, r1) of refined block B and project the matches, one
-// reservation of output rows per step of kENT x kRowsPerThread rows.
-__device__ void probe_rows(const EngineArgs & a, const Smem & sm, const uint8_t * B, uint32_t r0, uint32_t r1)
+// E2: one warp probes rows [r0, r1) of refined block B and projects the
+// matches, 256 rows a step with one reservation of output rows; a step's
+// output rows are placed round by round so each store instruction writes
+// consecutive rows.
+constexpr uint32_t kWarpRows = 8; // rows per lane per step
+__device__ void probe_rows_warp(const EngineArgs & a, const uint8_t * B, uint32_t r0, uint32_t r1, uint32_t lane)
 {
-    unsigned long long * out_slot = reinterpret_cast<unsigned long long *>(sm.scal + 10);
-    for (uint32_t base = r0; base < r1; base += kENT * kRowsPerThread)
+    const unsigned long long * keys = reinterpret_cast<const unsigned long long *>(B);
+    for (uint32_t base = r0; base < r1; base += 32 * kWarpRows)
     {
-        uint32_t head[kRowsPerThread], cnt[kRowsPerThread];
-        uint64_t key[kRowsPerThread];
-        uint32_t mine = 0;
+        uint64_t key[kWarpRows];
+        uint32_t head[kWarpRows], cnt[kWarpRows];
 #pragma unroll
-        for (uint32_t k = 0; k < kRowsPerThread; ++k)
+        for (uint32_t k = 0; k < kWarpRows; ++k)
         {
-            const uint32_t i = base + k * kENT + threadIdx.x;
-            cnt[k] = 0;
-            key[k] = 0;
-            head[k] = 0;
-            if (i < r1)
-            {
-                key[k] = __ldcg(reinterpret_cast<const unsigned long long *>(B) + i);
-                cnt[k] = lookup(a, key[k], head[k]);
-            }
-            mine += cnt[k];
+            const uint32_t i = base + k * 32 + lane;
+            key[k] = i < r1 ? __ldcg(keys + i) : 0ull;
         }
-        uint32_t total;
-        const uint32_t ex = block_excl_scan<kENT>(mine, sm.ws, &total);
-        if (threadIdx.x == 0)
-            *out_slot = total ? atomicAdd(&a.ctl->out_rows, (unsigned long long)total) : 0ull;
-        __syncthreads();
-        const uint64_t out0 = *reinterpret_cast<volatile unsigned long long *>(out_slot);
-        __syncthreads();
+#pragma unroll
+        for (uint32_t k = 0; k < kWarpRows; ++k)
+        {
+            const uint32_t i = base + k * 32 + lane;
+            head[k] = 0;
+            cnt[k] = i < r1 ? lookup(a, key[k], head[k]) : 0u;
+        }
+        // placement: a warp scan per round, rounds one after another
+        uint32_t rel[kWarpRows], total = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < kWarpRows; ++k)
+        {
+            uint32_t x = cnt[k];
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1)
+            {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, x, d);
+                if (lane >= (uint32_t)d)
+                    x += y;
+            }
+            rel[k] = total + x - cnt[k];
+            total += __shfl_sync(0xffffffffu, x, 31);
+        }
         if (total == 0)
             continue;
-        uint64_t o = out0 + ex;
+        unsigned long long out0 = 0;
+        if (lane == 0)
+            out0 = atomicAdd(&a.ctl->out_rows, (unsigned long long)total);
+        out0 = __shfl_sync(0xffffffffu, out0, 0);
 #pragma unroll 1
-        for (uint32_t k = 0; k < kRowsPerThread; ++k)
+        for (uint32_t k = 0; k < kWarpRows; ++k)
         {
             if (cnt[k] == 0)
                 continue;
-            const uint32_t i = base + k * kENT + threadIdx.x;
+            const uint32_t i = base + k * 32 + lane;
+            uint64_t o = out0 + rel[k];
             uint32_t b = head[k];
             for (uint32_t m = 0; m < cnt[k]; ++m, ++o)
             {
@@ -946,8 +1004,7 @@ __device__ bool evict_phase(const EngineArgs & a, const Smem & sm, uint32_t & ge
             a.ctl->work_n = total;
         __syncthreads();
     }
-    if (!build_claimed(a, sm))
-        return false;
+    build_claimed(a);
     if (!grid_sync(a, gen, NoOp{}))
         return false;
     // E1c: the refined blocks of the range's buckets into the work list
@@ -960,55 +1017,65 @@ __device__ bool evict_phase(const EngineArgs & a, const Smem & sm, uint32_t & ge
     if (!grid_sync(a, gen, NoOp{}))
         return false;
     const uint64_t t1 = now_ns();
-    // E2: probe the range's rows of every listed block
-    for (;;)
+    // E2: every warp takes a 1024-row part of a listed block at a time and
+    // probes the range's rows in it.  Parts are handed out in list order
+    // (bucket by bucket), so the warps in flight cover little more than one
+    // bucket and its leaf tables and build rows stay in L2.
     {
-        if (threadIdx.x == 0)
+        constexpr uint32_t kPart = 1024;
+        const uint32_t lane = threadIdx.x & 31;
+        const uint32_t parts = (1u << a.page_log2) > kPart ? (1u << a.page_log2) / kPart : 1u;
+        const uint32_t part_rows = (1u << a.page_log2) / parts;
+        const uint64_t n_items = (uint64_t)vload(&a.ctl->work_n) * parts;
+        for (;;)
         {
-            const uint32_t w = atomicAdd(&a.ctl->work_next, 1u);
-            sm.scal[8] = w < vload(&a.ctl->work_n) ? __ldcg(a.work + w) : kNone;
-        }
-        __syncthreads();
-        const uint32_t blk = sm.scal[8];
-        __syncthreads();
-        if (blk == kNone)
-            break;
-        const uint32_t p = __ldcg(a.blk_state + blk);
-        const uint32_t nrows = __ldcg(a.blk_rows + blk);
-        const uint32_t lf = __ldcg(a.blk_lfirst + blk), ll = __ldcg(a.blk_llast + blk);
-        const uint8_t * B = block_ptr(a, blk);
-        uint32_t x0, x1, y0, y1;
-        bucket_intervals(a, p, lo, block_len(a, __ldcg(a.blk_c0 + blk), lo_abs, len), x0, x1, y0, y1);
-        uint32_t done = 0;
-        for (int part = 0; part < 2; ++part)
-        {
-            const uint32_t l0 = part ? y0 : x0, l1 = part ? y1 : x1;
-            if (l1 <= l0 || l1 <= lf || l0 > ll)
-                continue; // no row of the block in these leaves
-            uint32_t ra = 0, rb = nrows;
-            if (l0 > lf || l1 <= ll)
+            unsigned long long w = 0;
+            if (lane == 0)
+                w = atomicAdd(&a.ctl->work_next, 1ull);
+            w = __shfl_sync(0xffffffffu, w, 0);
+            if (w >= n_items)
+                break;
+            const uint32_t blk = __ldcg(a.work + w / parts);
+            const uint32_t c0r = (uint32_t)(w % parts) * part_rows; // the part's first row
+            // (blk_state may already be cleared by the warp that probed the
+            // block's last rows; the bucket stays)
+            const uint32_t p = __ldcg(a.blk_bucket + blk);
+            const uint32_t nrows = __ldcg(a.blk_rows + blk);
+            if (c0r >= nrows)
+                continue;
+            const uint32_t c1r = c0r + part_rows < nrows ? c0r + part_rows : nrows;
+            const uint32_t lf = __ldcg(a.blk_lfirst + blk), ll = __ldcg(a.blk_llast + blk);
+            const uint8_t * B = block_ptr(a, blk);
+            uint32_t x0, x1, y0, y1;
+            bucket_intervals(a, p, lo, block_len(a, __ldcg(a.blk_c0 + blk), lo_abs, len), x0, x1, y0, y1);
+            uint32_t done = 0;
+            for (int part = 0; part < 2; ++part)
             {
-                leaf_bounds(a, sm, B, nrows, l0, l1);
-                ra = sm.scal[12];
-                rb = sm.scal[13];
-                __syncthreads();
+                const uint32_t l0 = part ? y0 : x0, l1 = part ? y1 : x1;
+                if (l1 <= l0 || l1 <= lf || l0 > ll)
+                    continue; // no row of the block in these leaves
+                uint32_t ra = l0 > lf ? lower_bound_warp(a, B, 0, nrows, l0, lane) : 0u;
+                uint32_t rb = l1 <= ll ? lower_bound_warp(a, B, ra, nrows, l1, lane) : nrows;
+                ra = ra > c0r ? ra : c0r;
+                rb = rb < c1r ? rb : c1r;
+                if (rb <= ra)
+                    continue;
+                probe_rows_warp(a, B, ra, rb, lane);
+                done += rb - ra;
             }
-            probe_rows(a, sm, B, ra, rb);
-            done += rb - ra;
-        }
-        if (threadIdx.x == 0 && done)
-        {
-            atomicAdd(&a.ctl->rows_probed, (unsigned long long)done);
-            const uint32_t left = atomicSub(a.blk_rem + blk, done) - done;
-            if (left == 0)
+            if (lane == 0 && done)
             {
-                // every row probed: the block goes back to the pool
-                a.blk_state[blk] = kNone;
-                const long long slot = (long long)atomicAdd(reinterpret_cast<unsigned long long *>(&a.ctl->free_top), 1ull);
-                a.free_stack[slot] = blk;
+                atomicAdd(&a.ctl->rows_probed, (unsigned long long)done);
+                const uint32_t left = atomicSub(a.blk_rem + blk, done) - done;
+                if (left == 0)
+                {
+                    // every row probed: the block goes back to the pool
+                    a.blk_state[blk] = kNone;
+                    const long long slot = (long long)atomicAdd(reinterpret_cast<unsigned long long *>(&a.ctl->free_top), 1ull);
+                    a.free_stack[slot] = blk;
+                }
             }
         }
-        __syncthreads();
     }
     const uint64_t t2 = now_ns();
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -1061,6 +1128,8 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
         p += (stage + 15) & ~15ull;
         sm.perm = reinterpret_cast<uint16_t *>(p);
         p += ((uint64_t)page * 2 + 15) & ~15ull;
+        sm.src = reinterpret_cast<uint16_t *>(p);
+        p += ((uint64_t)page * 2 + 15) & ~15ull;
         const uint32_t nbins = P1 > LB ? (P1 > page ? P1 : page) : (LB > page ? LB : page);
         sm.bins = reinterpret_cast<uint32_t *>(p);
         p += ((uint64_t)nbins * 4 + 15) & ~15ull;
@@ -1074,6 +1143,8 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
         p += ((uint64_t)P1 * 4 + 15) & ~15ull;
         sm.urows = reinterpret_cast<uint32_t *>(p);
         p += ((uint64_t)P1 * 4 + 15) & ~15ull;
+        sm.acc = reinterpret_cast<uint32_t *>(p);
+        p += ((uint64_t)LB * 4 + 15) & ~15ull;
         sm.ws = reinterpret_cast<uint32_t *>(p);
         p += (kENT / 32) * 4;
         sm.scal = reinterpret_cast<uint32_t *>(p);
@@ -1085,6 +1156,8 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
         sm.clen[p] = 0;
         sm.urows[p] = 0;
     }
+    for (uint32_t p = threadIdx.x; p < P1; p += kENT)
+        sm.bins[p] = 0;
     if (threadIdx.x < 32)
         sm.scal[threadIdx.x] = 0;
     __syncthreads();
@@ -1096,6 +1169,9 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
     {
         // -------- S: this wave's tile of the slice, then the refine trigger --------
         const uint64_t t0 = now_ns();
+        for (uint32_t p = threadIdx.x; p < P1; p += kENT)
+            sm.bins[p] = 0; // refines and E use the bins too
+        __syncthreads();
         const uint64_t end = umin64(hi, pos + a.tile_rows);
         while (pos < end)
         {
@@ -1201,12 +1277,12 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     a.leaf_low = a.leaf_high * 5 / 8;
     const uint64_t P1 = a.n_buckets, LB = 1ull << a.lb_log2;
     const uint64_t high_rows = a.unref_high / rb;
-    // block rows: a power of two, 64..4096, about what one bucket of a group
+    // block rows: a power of two, 64..8192, about what one bucket of a group
     // gathers before its group refines (so a refined block is mostly
     // full), and whose rows fit 96 KiB of shared memory (the refine sorts a
     // whole block there)
     uint32_t page_log2 = 6;
-    while (page_log2 < 12 && (2ull << page_log2) <= std::max<uint64_t>(high_rows / P1, 1))
+    while (page_log2 < 13 && (2ull << page_log2) <= std::max<uint64_t>(high_rows / P1, 1))
         ++page_log2;
     while (page_log2 > 6 && ((uint64_t)rb << page_log2) > (96u << 10))
         --page_log2;
@@ -1221,9 +1297,9 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     a.block_bytes = (off + 255) & ~255ull;
     a.smem_cells = (uint32_t)std::min<uint64_t>(4096, std::max<uint64_t>((page * rb) / sizeof(Cell), 2048));
     // input rows a group scatters between two looks at the global leaf
-    // count: half its unrefined high water, within [256, 16 blocks] (64K
-    // rows at 12-byte rows), so one wave overshoots the marks by little
-    a.tile_rows = std::min<uint64_t>(page * 16, std::max<uint64_t>(256, (high_rows / 2) & ~255ull));
+    // count: half its unrefined high water, within [256, 64K], so one wave
+    // overshoots the marks by little
+    a.tile_rows = std::min<uint64_t>(std::min<uint64_t>(page * 16, 65536), std::max<uint64_t>(256, (high_rows / 2) & ~255ull));
     const uint64_t slice = ceil_div(std::max<uint64_t>(in.probe_rows, 1), G);
     a.waves = (uint32_t)std::max<uint64_t>(1, ceil_div(slice, a.tile_rows));
     // pool, in blocks: a group's unrefined chains hold at most its high
@@ -1249,6 +1325,7 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     a.blk_rem = s.get<uint32_t>(a.n_blocks);
     a.blk_lfirst = s.get<uint32_t>(a.n_blocks);
     a.blk_llast = s.get<uint32_t>(a.n_blocks);
+    a.blk_bucket = s.get<uint32_t>(a.n_blocks);
     a.blk_c0 = s.get<unsigned long long>(a.n_blocks);
     a.chain = s.get<uint32_t>((uint64_t)G * P1 * a.maxb);
     a.leaf_rows = s.get<uint32_t>(a.n_leaves);
@@ -1275,8 +1352,8 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     // shared memory: stage, permutation, bins, the per-bucket state
     const uint64_t stage = std::max<uint64_t>(page * rb, (uint64_t)a.smem_cells * sizeof(Cell));
     const uint64_t nbins = std::max(std::max(P1, LB), page);
-    const size_t smem = ((stage + 15) & ~15ull) + ((page * 2 + 15) & ~15ull) + ((nbins * 4 + 15) & ~15ull) + 5 * ((P1 * 4 + 15) & ~15ull) +
-                        (kENT / 32) * 4 + 32 * 4;
+    const size_t smem = ((stage + 15) & ~15ull) + 2 * ((page * 2 + 15) & ~15ull) + ((nbins * 4 + 15) & ~15ull) + 5 * ((P1 * 4 + 15) & ~15ull) +
+                        ((LB * 4 + 15) & ~15ull) + (kENT / 32) * 4 + 32 * 4;
     if (smem + 1024 > (size_t)ctx->smem_optin)
         throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP): the device budget engine's shared memory does not fit this configuration");
     PHJ_CUDA(cudaFuncSetAttribute(k_bep_engine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
