@@ -532,6 +532,26 @@ def main():
         line["bep"]["budget_mib_per_group"] = BEP_BUDGET_PER_GROUP.get(args.workload, 32)
         line["bep"]["phase_ms"] = {k: getattr(res, k).wall_ms for k in
                                    ("build_shuffle", "build", "probe_shuffle", "probe", "eviction_overhead")}
+        line["bep"]["form"] = ("device budget engine (per-group unrefined chains, water marks, refinement, round-robin "
+                               "eviction, lazy builds)" if ctx.get_int("bep_engine") == 0 else "budget-sized probe batches")
+        # the other form on the same inputs: budget-sized probe batches
+        if ctx.get_int("bep_engine") == 0:
+            ctx.set_int("bep_engine", 1)
+            try:
+                out, _ = run_scheme(ctx, scheme, b, p, bits, budget)
+                out.free()
+                bms = []
+                for _ in range(3):
+                    ctx.flush_l2()
+                    out, bres = run_scheme(ctx, scheme, b, p, bits, budget)
+                    bms.append(bres.e2e_wall_ms)
+                    fp_b = out.fingerprint()
+                    out.free()
+            finally:
+                ctx.set_int("bep_engine", 0)
+            line["bep_batches"] = {"value": tuples / (statistics.mean(bms) / 1e3), "ms_per_step": statistics.mean(bms),
+                                   "fingerprint_equals_engine": fp_b == fp_main,
+                                   "bep_evictions": bres.bep_evictions, "bep_peak_bytes": bres.bep_peak_bytes}
 
     # -------- CHJ on the same inputs (extra line item) --------
     if not args.no_chj and scheme != "chj":
