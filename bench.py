@@ -93,9 +93,19 @@ def serve_once(reqs, arrivals, workers, batch_rows, batch_joins, budget):
     lat = np.array([r["done_s"] - r["arrival_s"] for r in recs])
     span = max(r["done_s"] for r in recs) - min(r["arrival_s"] for r in recs)
     tuples = sum(t for _, _, t in reqs)
+    # where a request's time goes: generating its inputs, the join call on
+    # the host (launches, host round trips, allocations) and the join's
+    # device time inside it
+    dev_s = sum(r["device_ms"] for r in recs) / 1e3
+    call_s = sum(r["call_s"] for r in recs)
+    gen_s = sum(r["gen_s"] for r in recs)
     return {"tuples_per_s": tuples / span, "makespan_s": span, "p50_ms": float(np.percentile(lat, 50) * 1e3),
             "p99_ms": float(np.percentile(lat, 99) * 1e3), "p999_ms": float(np.percentile(lat, 99.9) * 1e3),
-            "mean_batch": float(np.mean([r["batch_size"] for r in recs])), "requests": len(recs)}, recs
+            "mean_batch": float(np.mean([r["batch_size"] for r in recs])), "requests": len(recs),
+            "breakdown": {"join_device_s": dev_s, "join_call_s": call_s, "input_gen_s": gen_s,
+                          "join_device_busy_frac_of_makespan": dev_s / span,
+                          "call_overhead_ms_per_request": (call_s - dev_s) * 1e3 / len(recs),
+                          "device_tuples_per_s": tuples / dev_s if dev_s > 0 else None}}, recs
 
 
 def serving_benchmark(n_requests, workers=4, batch_rows=1 << 18, batch_joins=64, budget=150 << 30, seed=0xC5):
@@ -418,6 +428,8 @@ def main():
     ap.add_argument("--set", action="append", default=[], metavar="NAME=VALUE", help="context option (phj_ctx_set_int)")
     ap.add_argument("--serve-requests", type=int, default=2048, help="requests of the batched/served stream (0: skip it)")
     ap.add_argument("--serve-only", action="store_true", help="run only the batched/served stream")
+    ap.add_argument("--serve-batch-rows", type=int, default=1 << 18, help="served form: requests of at most this many build rows are batched")
+    ap.add_argument("--serve-slots", type=int, default=4, help="served form: execution slots (contexts with their own streams)")
     ap.add_argument("--csv", default=None, help="append the timed runs to this CSV (the reference's columns + GPU columns)")
     args = ap.parse_args()
     rank, world, local = env_rank()
@@ -426,7 +438,7 @@ def main():
         reference_arm(args, rank, world, dist)
         return
     if args.serve_only:
-        print(json.dumps({"serving": serving_benchmark(args.serve_requests)}), flush=True)
+        print(json.dumps({"serving": serving_benchmark(args.serve_requests, args.serve_slots, args.serve_batch_rows)}), flush=True)
         return
 
     import phj_gpu as P
@@ -667,7 +679,7 @@ def main():
     ctx.close()
     # -------- batched / served request stream versus the plain form --------
     if rank == 0 and args.serve_requests > 0:
-        line["batched_serving"] = serving_benchmark(args.serve_requests)
+        line["batched_serving"] = serving_benchmark(args.serve_requests, args.serve_slots, args.serve_batch_rows)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

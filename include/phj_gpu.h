@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PHJ_GPU_ABI_VERSION 2u
+#define PHJ_GPU_ABI_VERSION 3u
 #define PHJ_MAX_PAYLOADS 8u /* payload columns per side */
 
 /* Error codes.  The reference throws std::invalid_argument / std::bad_alloc
@@ -355,6 +355,9 @@ typedef struct phj_serve_record {
     uint32_t slot;
     int32_t status;                /* phj_status; -1 while not done */
     uint64_t job_peak_bytes;       /* measured peak device bytes of the launch set (inputs included) */
+    double gen_s;                  /* host seconds generating the request's inputs on the device */
+    double call_s;                 /* host seconds of the join call (its launch set's share when batched) */
+    double device_ms;              /* the join's device time, first kernel to last (its share when batched) */
 } phj_serve_record;
 
 typedef struct phj_server phj_server;

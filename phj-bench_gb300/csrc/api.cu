@@ -567,6 +567,13 @@ static void run_chj(phj_ctx * ctx, const phj_table & B, const phj_table & P, phj
     *out = o;
 }
 
+phj_output * join_alone(phj_ctx * ctx, const phj_table & B, const phj_table & P)
+{
+    phj_output * o = nullptr;
+    run_chj(ctx, B, P, &o, nullptr);
+    return o;
+}
+
 // Bits of the probe side's first (and only written) radix pass in PHJ-PURE.
 // The lookup takes every row's leaf from the whole hash, so this width is a
 // performance choice, not the configuration's: buckets narrow enough that

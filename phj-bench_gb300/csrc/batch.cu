@@ -1,19 +1,32 @@
-// batch.cu -- many independent joins in one set of launches.
+// batch.cu -- many independent joins in one persistent launch.
 //
-// A serving stream is dominated in count by small joins (a few thousand to a
-// few hundred thousand build rows).  Run one at a time, each pays a dozen
-// launches, two host round trips and grids too small to fill 152 SMs.  Here
-// n joins share every launch: a device descriptor per join, prefix sums of
-// their build tiles and probe warp chunks, and kernels whose work items are
-// (join, tile) or (join, chunk) pairs found by binary search in the prefix.
-//
-// Per join the algorithm is the global-table join: one open-addressing table
-// of bit_ceil(2 * build rows) 16-byte cells (the JoinHashTable layout,
-// src/HashTable.h:27-166) with the BlockStore next-chain per build row
-// (src/BlockStore.h:34-95), then lookups, an exact output size from a scan of
-// per-chunk match counts, and the projection (key, build payloads, probe
-// payloads: src/JoinOps.h:52-196).  Output multisets equal those of the
-// single-join entry points.
+// A serving stream is dominated in count by small and medium joins (a few
+// thousand to a few million build rows).  Run one at a time, each pays a
+// dozen launches, host round trips and grids too small to fill 152 SMs.
+// Here n joins share every launch:
+//   1. k_bt_hist     tiles of 4096 rows of every join's build and probe
+//                    side, found by binary search in their prefix: each
+//                    join's rows are counted per radix partition (the top
+//                    bits of intHash64, src/Hash.h:18-25; enough bits for
+//                    about 1024 build rows a partition, at most 11);
+//   2. scan_u32      the counts of all joins' partitions -> offsets;
+//   3. k_bt_scatter  the same tiles: each tile reserves its rows' places in
+//                    each partition with one atomic per partition and
+//                    writes them (src/RadixPartition.cpp:316-393);
+//   4. k_bt_join     ONE persistent launch whose CTAs pop (join, partition)
+//                    work items from a device queue (one atomic counter):
+//                    the partition's build rows go into a shared-memory
+//                    JoinHashTable with its next-chain (src/HashTable.h,
+//                    src/BlockStore.h), its probe rows are looked up there,
+//                    and the matches are projected (key, build payloads,
+//                    probe payloads: src/JoinOps.h:52-196) after one
+//                    reservation of output rows per step in the join's
+//                    output.  A partition with more build rows than the
+//                    shared table holds is built and probed in pieces.
+// Each join's output is sized for one row per probe row; a join with more
+// (repeated build keys) is counted exactly, flagged, and run again alone.
+// Output multisets equal those of the single-join entry points; the order
+// of the rows is not fixed.
 #include "internal.h"
 
 #include <numeric>
@@ -22,23 +35,23 @@ namespace phjg
 {
 namespace
 {
-constexpr int kBNT = 256;       // threads per CTA
-constexpr int kBTile = 256;     // build rows per tile (one per thread)
-constexpr int kBChunk = 256;    // probe rows per warp chunk
-constexpr int kBRPT = kBChunk / 32;
-constexpr uint32_t kBNoMatch = 0xFFFFFFFFu;
+constexpr int kTNT = 256;              // threads of the partition kernels
+constexpr uint32_t kTile = 4096;       // rows per partition tile
+constexpr int kJNT = 512;              // threads of the join kernel
+constexpr uint32_t kPieceRows = 2048;  // build rows a shared table holds
+constexpr uint32_t kPieceCells = 4096; // its cells (load <= 1/2)
+constexpr uint32_t kNil = 0xFFFFFFFFu;
 
 struct BatchJoin
 {
-    Cols build;        // keys + build payloads
-    Cols probe;        // keys + probe payloads
-    Cols out_b;        // keys = output key column, col[] = build payload outputs
-    Cols out_p;        // col[] = probe payload outputs
-    uint64_t build_rows, probe_rows;
-    uint64_t cell_off;   // first cell of the join's table
-    uint64_t build_base; // first slot of the join in the next-chain arena
-    uint64_t probe_base; // first slot of the join in the head arena
-    uint32_t log2cap;
+    Cols build, probe; // inputs
+    Cols bpart, ppart; // partitioned copies
+    uint64_t * out_keys;
+    void * out_l[kMaxCols];
+    void * out_r[kMaxCols];
+    uint64_t build_rows, probe_rows, out_cap;
+    uint32_t bits;      // radix bits
+    uint32_t part_base; // index of its first partition among all joins'
 };
 
 // Index j with pre[j] <= t < pre[j+1] (pre non-decreasing, pre[0] = 0).
@@ -56,155 +69,207 @@ __device__ __forceinline__ uint32_t find_join(const uint64_t * __restrict__ pre,
     return lo;
 }
 
-__global__ void k_batch_clear(Cell * __restrict__ cells, uint64_t n)
+__device__ __forceinline__ uint32_t part_of(uint64_t key, uint32_t bits)
 {
-    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
-        reinterpret_cast<ulonglong2 *>(cells)[i] = make_ulonglong2(0ull, INVALID_REF);
+    return bits ? (uint32_t)(int_hash64(key) >> (64u - bits)) : 0u;
 }
 
-__global__ void __launch_bounds__(kBNT) k_batch_build(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ tiles,
-                                                      Cell * __restrict__ cells, uint64_t * __restrict__ next)
+// Tile t of the build sides (t < tiles_b[n]) or of the probe sides.
+struct TileRef
 {
-    const uint64_t n_tiles = tiles[n];
+    const BatchJoin * J;
+    bool build;
+    uint64_t r0, r1;
+};
+__device__ __forceinline__ TileRef tile_ref(const BatchJoin * d, uint32_t n, const uint64_t * tb, const uint64_t * tp, uint64_t t)
+{
+    TileRef x;
+    const uint64_t nb = tb[n];
+    x.build = t < nb;
+    const uint64_t u = x.build ? t : t - nb;
+    const uint32_t j = find_join(x.build ? tb : tp, n, u);
+    x.J = d + j;
+    x.r0 = (u - (x.build ? tb : tp)[j]) * kTile;
+    const uint64_t rows = x.build ? x.J->build_rows : x.J->probe_rows;
+    x.r1 = x.r0 + kTile < rows ? x.r0 + kTile : rows;
+    return x;
+}
+
+__global__ void __launch_bounds__(kTNT) k_bt_hist(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ tb,
+                                                  const uint64_t * __restrict__ tp, uint32_t * __restrict__ cnt_b, uint32_t * __restrict__ cnt_p)
+{
+    __shared__ uint32_t h[1u << 11];
+    const uint64_t n_tiles = tb[n] + tp[n];
     for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x)
     {
-        const uint32_t j = find_join(tiles, n, t);
-        const BatchJoin & J = d[j];
-        const uint64_t r = (t - tiles[j]) * kBTile + threadIdx.x;
-        if (r < J.build_rows)
-        {
-            const uint64_t k = J.build.keys[r];
-            next[J.build_base + r] = table_insert<false>(cells + J.cell_off, 1ull << J.log2cap, int_hash64(k), k, make_ref(0, (uint32_t)r));
-        }
+        const TileRef x = tile_ref(d, n, tb, tp, t);
+        const uint32_t Q = 1u << x.J->bits;
+        for (uint32_t q = threadIdx.x; q < Q; q += kTNT)
+            h[q] = 0;
+        __syncthreads();
+        const uint64_t * keys = x.build ? x.J->build.keys : x.J->probe.keys;
+        for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += kTNT)
+            atomicAdd(&h[part_of(keys[r], x.J->bits)], 1u);
+        __syncthreads();
+        uint32_t * cnt = (x.build ? cnt_b : cnt_p) + x.J->part_base;
+        for (uint32_t q = threadIdx.x; q < Q; q += kTNT)
+            if (h[q])
+                atomicAdd(cnt + q, h[q]);
+        __syncthreads();
     }
 }
 
-__device__ __forceinline__ uint32_t chain_len(const uint64_t * __restrict__ next, uint64_t base, uint32_t head)
+// Rows of the tile to their partitions: one reservation per partition and
+// tile on the running cursors (offsets over all joins' partitions), the
+// row's rank inside the tile's share from a shared counter.
+__global__ void __launch_bounds__(kTNT) k_bt_scatter(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ tb,
+                                                     const uint64_t * __restrict__ tp, const uint32_t * __restrict__ off_b,
+                                                     const uint32_t * __restrict__ off_p, uint32_t * __restrict__ cur_b,
+                                                     uint32_t * __restrict__ cur_p)
 {
-    uint32_t c = 1;
-    for (uint64_t r = __ldg(next + base + head); ref_valid(r); r = __ldg(next + base + ref_row(r)))
-        ++c;
-    return c;
-}
-
-// A warp per chunk of 256 probe rows: heads, and the chunk's output rows.
-// The batch's output rows are also summed in 64 bits (one atomic per warp),
-// so the host can refuse a batch whose 32-bit chunk offsets would wrap.
-__global__ void __launch_bounds__(kBNT) k_batch_lookup(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ chunks,
-                                                       const Cell * __restrict__ cells, const uint64_t * __restrict__ next,
-                                                       uint32_t * __restrict__ heads, uint32_t * __restrict__ counts,
-                                                       unsigned long long * __restrict__ out_rows64)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t n_chunks = chunks[n];
-    const uint64_t warps = ((uint64_t)gridDim.x * kBNT) >> 5;
-    unsigned long long warp_rows = 0;
-    for (uint64_t c = ((uint64_t)blockIdx.x * kBNT + threadIdx.x) >> 5; c < n_chunks; c += warps)
+    __shared__ uint32_t h[1u << 11];
+    __shared__ uint32_t base[1u << 11];
+    const uint64_t n_tiles = tb[n] + tp[n];
+    for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x)
     {
-        const uint32_t j = find_join(chunks, n, c);
-        const BatchJoin & J = d[j];
-        const uint64_t cap = 1ull << J.log2cap;
-        const Cell * tab = cells + J.cell_off;
-        const uint64_t row0 = (c - chunks[j]) * kBChunk + lane;
-        unsigned long long total = 0;
-#pragma unroll 4
-        for (int k = 0; k < kBRPT; ++k)
+        const TileRef x = tile_ref(d, n, tb, tp, t);
+        const uint32_t Q = 1u << x.J->bits;
+        for (uint32_t q = threadIdx.x; q < Q; q += kTNT)
+            h[q] = 0;
+        __syncthreads();
+        const Cols & src = x.build ? x.J->build : x.J->probe;
+        const Cols & dst = x.build ? x.J->bpart : x.J->ppart;
+        for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += kTNT)
+            atomicAdd(&h[part_of(src.keys[r], x.J->bits)], 1u);
+        __syncthreads();
+        // this tile's places in each partition, as rows of the join's
+        // partitioned columns
+        const uint32_t * off = (x.build ? off_b : off_p) + x.J->part_base;
+        uint32_t * cur = (x.build ? cur_b : cur_p) + x.J->part_base;
+        const uint32_t first = off[0];
+        for (uint32_t q = threadIdx.x; q < Q; q += kTNT)
         {
-            const uint64_t r = row0 + (uint64_t)k * 32;
-            if (r >= J.probe_rows)
-                break;
-            const uint64_t key = __ldcs(J.probe.keys + r);
-            const uint64_t h = table_find(tab, cap, int_hash64(key), key);
-            uint32_t head = kBNoMatch;
-            if (ref_valid(h))
-            {
-                head = ref_row(h);
-                total += chain_len(next, J.build_base, head);
-            }
-            heads[J.probe_base + r] = head;
+            base[q] = h[q] ? atomicAdd(cur + q, h[q]) - first : 0u;
+            h[q] = 0;
         }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1)
-            total += __shfl_xor_sync(0xffffffffu, total, o);
-        if (lane == 0)
-            counts[c] = (uint32_t)min(total, 0xFFFFFFFFull); // the host refuses the batch above 2^32 - 1 rows
-        warp_rows += total;
-    }
-    if (lane == 0 && warp_rows)
-        atomicAdd(out_rows64, warp_rows);
-}
-
-__global__ void k_batch_totals(const uint64_t * __restrict__ chunks, const uint32_t * __restrict__ offs, uint32_t n, uint64_t * __restrict__ totals)
-{
-    const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j < n)
-        totals[j] = (uint64_t)offs[chunks[j + 1]] - offs[chunks[j]];
-}
-
-// Output row o of join J: the probe key, the build payloads of build row b,
-// the probe payloads of probe row p.
-__device__ __forceinline__ void emit(const BatchJoin & J, uint64_t o, uint64_t key, uint32_t b, uint64_t p)
-{
-    J.out_b.keys[o] = key;
-    for (uint32_t c = 0; c < J.build.n; ++c)
-        copy_elem(J.out_b.col[c], o, J.build.col[c], b, J.build.width[c]);
-    for (uint32_t c = 0; c < J.probe.n; ++c)
-        copy_elem(J.out_p.col[c], o, J.probe.col[c], p, J.probe.width[c]);
-}
-
-__global__ void __launch_bounds__(kBNT) k_batch_project(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ chunks,
-                                                        const uint64_t * __restrict__ next, const uint32_t * __restrict__ heads,
-                                                        const uint32_t * __restrict__ offs)
-{
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t n_chunks = chunks[n];
-    const uint64_t warps = ((uint64_t)gridDim.x * kBNT) >> 5;
-    for (uint64_t c = ((uint64_t)blockIdx.x * kBNT + threadIdx.x) >> 5; c < n_chunks; c += warps)
-    {
-        const uint32_t j = find_join(chunks, n, c);
-        const BatchJoin & J = d[j];
-        uint64_t base = (uint64_t)offs[c] - offs[chunks[j]];
-        const uint64_t row0 = (c - chunks[j]) * kBChunk + lane;
-        for (int k = 0; k < kBRPT; ++k)
+        __syncthreads();
+        for (uint64_t r = x.r0 + threadIdx.x; r < x.r1; r += kTNT)
         {
-            const uint64_t r = row0 + (uint64_t)k * 32;
-            if (__all_sync(0xffffffffu, r >= J.probe_rows))
-                break;
-            uint32_t head = kBNoMatch, cnt = 0;
-            if (r < J.probe_rows)
+            const uint64_t k = src.keys[r];
+            const uint32_t q = part_of(k, x.J->bits);
+            const uint32_t pos = base[q] + atomicAdd(&h[q], 1u);
+            dst.keys[pos] = k;
+            for (uint32_t c = 0; c < src.n; ++c)
+                copy_elem(dst.col[c], pos, src.col[c], r, src.width[c]);
+        }
+        __syncthreads();
+    }
+}
+
+// The persistent join: CTAs pop (join, partition) items until the queue is
+// empty.  out_cur[j] counts join j's output rows (also past its capacity,
+// where nothing is written and over[j] is set).
+__global__ void __launch_bounds__(kJNT) k_bt_join(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ parts,
+                                                  const uint32_t * __restrict__ off_b, const uint32_t * __restrict__ off_p,
+                                                  unsigned int * __restrict__ next_item, unsigned long long * __restrict__ out_cur,
+                                                  int * __restrict__ over)
+{
+    __shared__ Cell cells[kPieceCells];
+    __shared__ uint32_t nxt[kPieceRows];
+    __shared__ uint32_t ws[kJNT / 32];
+    __shared__ uint32_t s_item;
+    __shared__ unsigned long long s_out;
+    const uint64_t n_items = parts[n];
+    for (;;)
+    {
+        if (threadIdx.x == 0)
+            s_item = atomicAdd(next_item, 1u);
+        __syncthreads();
+        const uint64_t item = s_item;
+        __syncthreads();
+        if (item >= n_items)
+            return;
+        const uint32_t j = find_join(parts, n, item);
+        const BatchJoin & J = d[j];
+        const uint32_t g = J.part_base + (uint32_t)(item - parts[j]);
+        const uint32_t b0 = off_b[g] - off_b[J.part_base], b1 = off_b[g + 1] - off_b[J.part_base];
+        const uint32_t p0 = off_p[g] - off_p[J.part_base], p1 = off_p[g + 1] - off_p[J.part_base];
+        if (b1 == b0 || p1 == p0)
+            continue;
+        // the partition's build rows, a piece at a time
+        for (uint32_t c0 = b0; c0 < b1; c0 += kPieceRows)
+        {
+            const uint32_t c1 = c0 + kPieceRows < b1 ? c0 + kPieceRows : b1;
+            const uint32_t cap = (uint32_t)bit_ceil64(2ull * (c1 - c0));
+            for (uint32_t i = threadIdx.x; i < cap; i += kJNT)
+                reinterpret_cast<ulonglong2 *>(cells)[i] = make_ulonglong2(0ull, INVALID_REF);
+            __syncthreads();
+            for (uint32_t r = c0 + threadIdx.x; r < c1; r += kJNT)
             {
-                head = heads[J.probe_base + r];
-                if (head != kBNoMatch)
-                    cnt = chain_len(next, J.build_base, head);
+                const uint64_t k = J.bpart.keys[r];
+                const uint64_t prev = table_insert<true>(cells, cap, int_hash64(k), k, make_ref(0, r));
+                nxt[r - c0] = ref_valid(prev) ? ref_row(prev) : kNil;
             }
-            uint32_t x = cnt;
-#pragma unroll
-            for (int s = 1; s < 32; s <<= 1)
+            __syncthreads();
+            // its probe rows: count, reserve, project
+            for (uint32_t base = p0; base < p1; base += kJNT)
             {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, x, s);
-                if (lane >= (uint32_t)s)
-                    x += y;
-            }
-            const uint64_t o0 = base + x - cnt;
-            base += __shfl_sync(0xffffffffu, x, 31);
-            if (cnt)
-            {
-                const uint64_t key = J.probe.keys[r];
-                uint32_t b = head;
-                for (uint32_t i = 0; i < cnt; ++i)
+                const uint32_t r = base + threadIdx.x;
+                uint64_t key = 0;
+                uint32_t head = kNil, cnt = 0;
+                if (r < p1)
                 {
-                    emit(J, o0 + i, key, b, r);
-                    const uint64_t nx = __ldg(next + J.build_base + b);
-                    b = ref_row(nx);
+                    key = J.ppart.keys[r];
+                    const uint64_t h = int_hash64(key);
+                    const uint64_t mask = cap - 1;
+                    uint64_t pos = probe_start(h, cap);
+                    for (uint32_t step = 0; step < cap; ++step)
+                    {
+                        const Cell c = cells[pos];
+                        if (!ref_valid(c.ref))
+                            break;
+                        if (c.key == key)
+                        {
+                            head = ref_row(c.ref);
+                            break;
+                        }
+                        pos = (pos + 1) & mask;
+                    }
+                    for (uint32_t b = head; b != kNil; b = nxt[b - c0])
+                        ++cnt;
                 }
+                uint32_t total;
+                const uint32_t ex = block_excl_scan<kJNT>(cnt, ws, &total);
+                if (total == 0)
+                    continue;
+                if (threadIdx.x == 0)
+                    s_out = atomicAdd(out_cur + j, (unsigned long long)total);
+                __syncthreads();
+                const uint64_t o0 = s_out + ex;
+                if (threadIdx.x == 0 && s_out + total > J.out_cap)
+                    over[j] = 1;
+                uint64_t o = o0;
+                for (uint32_t b = head; b != kNil; b = nxt[b - c0], ++o)
+                    if (o < J.out_cap)
+                    {
+                        J.out_keys[o] = key;
+                        for (uint32_t c = 0; c < J.bpart.n; ++c)
+                            copy_elem(J.out_l[c], o, J.bpart.col[c], b, J.bpart.width[c]);
+                        for (uint32_t c = 0; c < J.ppart.n; ++c)
+                            copy_elem(J.out_r[c], o, J.ppart.col[c], r, J.ppart.width[c]);
+                    }
+                __syncthreads(); // s_out is reused by the next step
             }
         }
     }
 }
 
-unsigned grid_for(phj_ctx * ctx, uint64_t items_per_cta_units)
+uint32_t partition_bits(uint64_t build_rows)
 {
-    return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(items_per_cta_units, (uint64_t)ctx->num_sms * 8));
+    uint32_t b = 0;
+    while (b < 11 && (build_rows >> b) > 1024)
+        ++b;
+    return b;
 }
 
 void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, const phj_table * const * probes, phj_output ** outs,
@@ -214,8 +279,8 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
     {
         if (!builds[j] || !probes[j])
             throw Error(PHJ_ERR_INVALID_ARGUMENT, "batch: null build or probe table");
-        if (builds[j]->rows >= (1ull << 31) || probes[j]->rows >= (1ull << 32))
-            throw Error(PHJ_ERR_UNSUPPORTED, "batch: < 2^31 build rows and < 2^32 probe rows per join");
+        if (builds[j]->rows >= (1ull << 31) || probes[j]->rows >= (1ull << 31))
+            throw Error(PHJ_ERR_UNSUPPORTED, "batch: fewer than 2^31 build rows and 2^31 probe rows per join");
     }
     begin_run(ctx);
     Scratch s(ctx);
@@ -223,8 +288,8 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
     PHJ_CUDA(cudaEventRecord(e0, ctx->stream));
 
     std::vector<BatchJoin> h(n);
-    std::vector<uint64_t> tiles(n + 1, 0), chunks(n + 1, 0);
-    uint64_t cells = 0, brows = 0, prows = 0;
+    std::vector<uint64_t> tb(n + 1, 0), tp(n + 1, 0), parts(n + 1, 0);
+    uint64_t brows = 0, prows = 0;
     for (uint32_t j = 0; j < n; ++j)
     {
         const phj_table & B = *builds[j];
@@ -235,91 +300,109 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
         J.probe = cols_of(P);
         J.build_rows = B.rows;
         J.probe_rows = P.rows;
-        const uint64_t cap = B.rows ? bit_ceil64(2 * B.rows) : 1;
-        J.log2cap = (uint32_t)__builtin_ctzll(cap);
-        J.cell_off = cells;
-        J.build_base = brows;
-        J.probe_base = prows;
-        cells += cap;
+        J.bits = partition_bits(B.rows);
+        J.part_base = (uint32_t)parts[j];
+        J.bpart = alloc_cols_like(s, B.schema, std::max<uint64_t>(B.rows, 1));
+        J.ppart = alloc_cols_like(s, P.schema, std::max<uint64_t>(P.rows, 1));
+        parts[j + 1] = parts[j] + (1ull << J.bits);
+        tb[j + 1] = tb[j] + ceil_div(B.rows, kTile);
+        tp[j + 1] = tp[j] + ceil_div(P.rows, kTile);
         brows += B.rows;
         prows += P.rows;
-        tiles[j + 1] = tiles[j] + ceil_div(B.rows, kBTile);
-        chunks[j + 1] = chunks[j] + ceil_div(P.rows, kBChunk);
     }
-    Cell * d_cells = s.get<Cell>(std::max<uint64_t>(cells, 1));
-    uint64_t * d_next = s.get<uint64_t>(std::max<uint64_t>(brows, 1));
-    uint32_t * d_heads = s.get<uint32_t>(std::max<uint64_t>(prows, 1));
-    uint32_t * d_counts = s.get<uint32_t>(chunks[n] + 1);
-    uint64_t * d_tiles = s.get<uint64_t>(n + 1);
-    uint64_t * d_chunks = s.get<uint64_t>(n + 1);
-    uint64_t * d_totals = s.get<uint64_t>(std::max<uint32_t>(n, 1));
-    unsigned long long * d_rows64 = s.get<unsigned long long>(1);
-    PHJ_CUDA(cudaMemsetAsync(d_rows64, 0, sizeof(unsigned long long), ctx->stream));
+    if (brows >= (1ull << 32) || prows >= (1ull << 32))
+        throw Error(PHJ_ERR_UNSUPPORTED, "batch: fewer than 2^32 build rows and 2^32 probe rows in all");
+    const uint64_t NQ = parts[n];
+    uint32_t * cnt_b = s.get<uint32_t>(NQ + 1);
+    uint32_t * cnt_p = s.get<uint32_t>(NQ + 1);
+    uint32_t * off_b = s.get<uint32_t>(NQ + 1);
+    uint32_t * off_p = s.get<uint32_t>(NQ + 1);
+    uint32_t * cur_b = s.get<uint32_t>(NQ + 1);
+    uint32_t * cur_p = s.get<uint32_t>(NQ + 1);
+    uint64_t * d_tb = s.get<uint64_t>(n + 1);
+    uint64_t * d_tp = s.get<uint64_t>(n + 1);
+    uint64_t * d_parts = s.get<uint64_t>(n + 1);
+    unsigned int * next_item = s.get<unsigned int>(1);
+    unsigned long long * out_cur = s.get<unsigned long long>(std::max<uint32_t>(n, 1));
+    int * over = s.get<int>(std::max<uint32_t>(n, 1));
     BatchJoin * d_desc = s.get<BatchJoin>(std::max<uint32_t>(n, 1));
-    PHJ_CUDA(cudaMemcpyAsync(d_tiles, tiles.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(d_chunks, chunks.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(d_desc, h.data(), n * sizeof(BatchJoin), cudaMemcpyHostToDevice, ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(cnt_b, 0, (NQ + 1) * sizeof(uint32_t), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(cnt_p, 0, (NQ + 1) * sizeof(uint32_t), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(next_item, 0, sizeof(unsigned int), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(out_cur, 0, std::max<uint32_t>(n, 1) * sizeof(unsigned long long), ctx->stream));
+    PHJ_CUDA(cudaMemsetAsync(over, 0, std::max<uint32_t>(n, 1) * sizeof(int), ctx->stream));
+    PHJ_CUDA(cudaMemcpyAsync(d_tb, tb.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+    PHJ_CUDA(cudaMemcpyAsync(d_tp, tp.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
+    PHJ_CUDA(cudaMemcpyAsync(d_parts, parts.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
 
-    {
-        KTimer kt(ctx, "batch_clear", cells, cells * sizeof(Cell));
-        k_batch_clear<<<grid_for(ctx, ceil_div(cells, kBNT)), kBNT, 0, ctx->stream>>>(d_cells, cells);
-        PHJ_LAUNCHED(ctx, "batch_clear");
-    }
-    if (tiles[n])
-    {
-        KTimer kt(ctx, "batch_build", brows, brows * (8 + 16 + 8));
-        k_batch_build<<<grid_for(ctx, tiles[n]), kBNT, 0, ctx->stream>>>(d_desc, n, d_tiles, d_cells, d_next);
-        PHJ_LAUNCHED(ctx, "batch_build");
-    }
-    std::vector<uint64_t> totals(n, 0);
-    if (chunks[n])
-    {
-        {
-            KTimer kt(ctx, "batch_lookup", prows, prows * (8 + 4));
-            k_batch_lookup<<<grid_for(ctx, ceil_div(chunks[n], kBNT / 32)), kBNT, 0, ctx->stream>>>(d_desc, n, d_chunks, d_cells, d_next, d_heads,
-                                                                                                     d_counts, d_rows64);
-            PHJ_LAUNCHED(ctx, "batch_lookup");
-        }
-        scan_u32(ctx, s, d_counts, d_counts, chunks[n]);
-        k_batch_totals<<<(unsigned)ceil_div(n, 256), 256, 0, ctx->stream>>>(d_chunks, d_counts, n, d_totals);
-        PHJ_LAUNCHED(ctx, "batch_totals");
-        unsigned long long rows64 = 0;
-        PHJ_CUDA(cudaMemcpyAsync(totals.data(), d_totals, n * sizeof(uint64_t), cudaMemcpyDeviceToHost, ctx->stream));
-        PHJ_CUDA(cudaMemcpyAsync(&rows64, d_rows64, sizeof(rows64), cudaMemcpyDeviceToHost, ctx->stream));
-        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
-        if (rows64 >= (1ull << 32))
-            throw Error(PHJ_ERR_CAPACITY, "the batch has " + std::to_string(rows64) +
-                                              " output rows; batched joins place at most 2^32 - 1 in all (run large joins on their own)");
-    }
+    // outputs at one row per probe row (exact for unique build keys)
     std::vector<phj_output *> made(n, nullptr);
     try
     {
-        uint64_t out_rows = 0, out_bytes = 0;
         for (uint32_t j = 0; j < n; ++j)
         {
-            made[j] = new_output(ctx, builds[j]->schema, probes[j]->schema, totals[j]);
-            made[j]->rows = totals[j];
+            made[j] = new_output(ctx, builds[j]->schema, probes[j]->schema, probes[j]->rows);
             BatchJoin & J = h[j];
-            J.out_b = J.build;
-            J.out_b.keys = made[j]->keys;
+            J.out_keys = made[j]->keys;
             for (uint32_t c = 0; c < J.build.n; ++c)
-                J.out_b.col[c] = made[j]->lcol[c];
-            J.out_p = J.probe;
-            J.out_p.keys = nullptr;
+                J.out_l[c] = made[j]->lcol[c];
             for (uint32_t c = 0; c < J.probe.n; ++c)
-                J.out_p.col[c] = made[j]->rcol[c];
-            out_rows += totals[j];
-            out_bytes += made[j]->bytes;
+                J.out_r[c] = made[j]->rcol[c];
+            J.out_cap = probes[j]->rows;
         }
-        if (chunks[n])
+        PHJ_CUDA(cudaMemcpyAsync(d_desc, h.data(), n * sizeof(BatchJoin), cudaMemcpyHostToDevice, ctx->stream));
+        const uint64_t n_tiles = tb[n] + tp[n];
+        const unsigned tgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->num_sms * 8));
+        if (n_tiles)
         {
-            PHJ_CUDA(cudaMemcpyAsync(d_desc, h.data(), n * sizeof(BatchJoin), cudaMemcpyHostToDevice, ctx->stream));
+            {
+                KTimer kt(ctx, "batch_hist", brows + prows, (brows + prows) * 8);
+                k_bt_hist<<<tgrid, kTNT, 0, ctx->stream>>>(d_desc, n, d_tb, d_tp, cnt_b, cnt_p);
+                PHJ_LAUNCHED(ctx, "batch_hist");
+            }
+            scan_u32(ctx, s, cnt_b, off_b, NQ);
+            scan_u32(ctx, s, cnt_p, off_p, NQ);
+            PHJ_CUDA(cudaMemcpyAsync(cur_b, off_b, (NQ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
+            PHJ_CUDA(cudaMemcpyAsync(cur_p, off_p, (NQ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
             uint64_t in_bytes = 0;
             for (uint32_t j = 0; j < n; ++j)
-                in_bytes += totals[j] * (8 + schema_bytes(probes[j]->schema));
-            KTimer kt(ctx, "batch_project", prows, prows * 4 + in_bytes + out_bytes);
-            k_batch_project<<<grid_for(ctx, ceil_div(chunks[n], kBNT / 32)), kBNT, 0, ctx->stream>>>(d_desc, n, d_chunks, d_next, d_heads, d_counts);
-            PHJ_LAUNCHED(ctx, "batch_project");
+                in_bytes += builds[j]->rows * (8 + schema_bytes(builds[j]->schema)) + probes[j]->rows * (8 + schema_bytes(probes[j]->schema));
+            {
+                KTimer kt(ctx, "batch_scatter", brows + prows, 2 * in_bytes);
+                k_bt_scatter<<<tgrid, kTNT, 0, ctx->stream>>>(d_desc, n, d_tb, d_tp, off_b, off_p, cur_b, cur_p);
+                PHJ_LAUNCHED(ctx, "batch_scatter");
+            }
+            int per_sm = 0;
+            PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bt_join, kJNT, 0));
+            const unsigned jgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(NQ, (uint64_t)ctx->num_sms * std::max(per_sm, 1)));
+            {
+                KTimer kt(ctx, "batch_join", prows, in_bytes);
+                k_bt_join<<<jgrid, kJNT, 0, ctx->stream>>>(d_desc, n, d_parts, off_b, off_p, next_item, out_cur, over);
+                PHJ_LAUNCHED(ctx, "batch_join");
+            }
+        }
+        std::vector<unsigned long long> rows(n, 0);
+        std::vector<int> ov(n, 0);
+        if (n)
+        {
+            PHJ_CUDA(cudaMemcpyAsync(rows.data(), out_cur, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
+            PHJ_CUDA(cudaMemcpyAsync(ov.data(), over, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+        uint64_t out_rows = 0;
+        for (uint32_t j = 0; j < n; ++j)
+        {
+            if (ov[j])
+            {
+                // more output rows than probe rows (repeated build keys):
+                // this join again, alone
+                free_output(ctx, made[j]);
+                made[j] = nullptr;
+                made[j] = join_alone(ctx, *builds[j], *probes[j]);
+            }
+            else
+                made[j]->rows = rows[j];
+            out_rows += made[j]->rows;
         }
         PHJ_CUDA(cudaEventRecord(e1, ctx->stream));
         PHJ_CUDA(cudaEventSynchronize(e1));
@@ -336,7 +419,8 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
     catch (...)
     {
         for (phj_output * o : made)
-            free_output(ctx, o);
+            if (o)
+                free_output(ctx, o);
         throw;
     }
     for (uint32_t j = 0; j < n; ++j)

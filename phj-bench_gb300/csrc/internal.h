@@ -353,6 +353,10 @@ bool bep_engine_supported(uint32_t b1, uint32_t total_bits);
 // One engine run into `out` (rows past out->cap are counted, not written).
 BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput & in, phj_output * out);
 
+// One join on its own (the CHJ scheme), for a batched join that needs more
+// output rows than the batch gave it.
+phj_output * join_alone(phj_ctx * ctx, const phj_table & B, const phj_table & P);
+
 // Lookups, then an exactly sized output, then the projection.
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right);
 // Sets a.packed (and packed_off) when the plain projection can use packed

@@ -70,8 +70,8 @@ uint64_t side_row_bytes(const phj_schema & s)
 
 // Estimated device bytes a request holds while it runs: its inputs, the
 // table (cells at load <= 1/2 plus the next-chain), the partition buffers of
-// a join run alone (both sides' shuffles) or the lookup heads of a batched
-// one, and an output of one row per probe row.
+// a join run alone (both sides' shuffles) or the partitioned copies of a
+// batched one, and an output of one row per probe row.
 uint64_t estimate_footprint(const phj_serve_request & r, bool batched)
 {
     const uint64_t B = r.build.rows, P = r.probe.rows;
@@ -79,7 +79,7 @@ uint64_t estimate_footprint(const phj_serve_request & r, bool batched)
     const uint64_t cells = B ? bit_ceil64(2 * B) : 1;
     const uint64_t in = B * rb + P * rp;
     const uint64_t table = cells * 16 + B * 8;
-    const uint64_t buffers = batched ? P * 4 : 2 * B * rb + P * rp + P * 4;
+    const uint64_t buffers = batched ? B * rb + P * rp : 2 * B * rb + P * rp + P * 4;
     const uint64_t out = P * (rb + rp - 8);
     return in + table + buffers + out;
 }
@@ -106,6 +106,10 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
         if (s == PHJ_OK)
             s = phj_table_generate(ctx, &S.reqs[job[i]].probe, &p[i]);
     }
+    if (s == PHJ_OK && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        s = PHJ_ERR_CUDA;
+    const double t_gen = S.now_s();
+    double device_ms = 0.0;
     if (s == PHJ_OK)
     {
         if (n == 1)
@@ -115,11 +119,18 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
             std::copy(S.cfg.pass_bits, S.cfg.pass_bits + 8, bits);
             if (np == 0)
                 phj_autotune_radix(S.reqs[job[0]].build.rows, S.reqs[job[0]].probe.rows, bits, &np);
-            s = phj_run_phj_pure(ctx, b[0], p[0], bits, np, &o[0], nullptr);
+            phj_phj_result r{};
+            s = phj_run_phj_pure(ctx, b[0], p[0], bits, np, &o[0], &r);
+            device_ms = r.e2e_wall_ms;
         }
         else
-            s = phj_batch_run(ctx, (uint32_t)n, b.data(), p.data(), o.data(), nullptr);
+        {
+            phj_batch_result r{};
+            s = phj_batch_run(ctx, (uint32_t)n, b.data(), p.data(), o.data(), &r);
+            device_ms = r.e2e_wall_ms;
+        }
     }
+    const double t_call = S.now_s();
     const uint64_t job_peak = ctx->peak_bytes; // the scheme run's peak, inputs and outputs included
     for (size_t i = 0; i < n; ++i)
     {
@@ -146,6 +157,9 @@ void run_job(phj_server & S, uint32_t slot, const std::vector<uint64_t> & job)
             r.fingerprint[k] = fp[i][k];
         r.output_rows = fp[i][0];
         r.job_peak_bytes = job_peak;
+        r.gen_s = (t_gen - t_start) / (double)n;
+        r.call_s = (t_call - t_gen) / (double)n;
+        r.device_ms = device_ms / (double)n;
         S.inflight_bytes -= S.footprint[job[i]];
         S.inflight_requests -= 1;
         ++S.completed;
@@ -191,14 +205,20 @@ std::vector<uint64_t> pick(phj_server & S)
         return job;
     }
     // continuous batching: every small ready request that fits, oldest first
-    uint64_t bytes = 0;
+    // (a batch holds fewer than 2^31 rows on each side)
+    uint64_t bytes = 0, brows = 0, prows = 0;
+    const uint64_t row_cap = 1ull << 31;
     for (auto it = S.ready.begin(); it != S.ready.end() && job.size() < S.cfg.batch_max_joins;)
     {
         const uint64_t id = *it;
-        if (is_small(S, id) && (job.empty() ? fits(S.footprint[id]) : S.inflight_bytes + bytes + S.footprint[id] <= S.cfg.hbm_budget_bytes))
+        const bool rows_fit = job.empty() || (brows + S.reqs[id].build.rows < row_cap && prows + S.reqs[id].probe.rows < row_cap);
+        if (is_small(S, id) && rows_fit &&
+            (job.empty() ? fits(S.footprint[id]) : S.inflight_bytes + bytes + S.footprint[id] <= S.cfg.hbm_budget_bytes))
         {
             job.push_back(id);
             bytes += S.footprint[id];
+            brows += S.reqs[id].build.rows;
+            prows += S.reqs[id].probe.rows;
             it = S.ready.erase(it);
         }
         else if (!is_small(S, id))

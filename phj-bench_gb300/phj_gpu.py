@@ -22,7 +22,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.environ.get("PHJ_GPU_LIB") or os.path.join(HERE, "libphj_gpu.so")
 MAX_PAYLOADS = 8
-ABI_VERSION = 2  # PHJ_GPU_ABI_VERSION of include/phj_gpu.h these structures follow
+ABI_VERSION = 3  # PHJ_GPU_ABI_VERSION of include/phj_gpu.h these structures follow
 
 # PayloadType codes, src/Types.h:23-30
 U8, U16, U32, U64, U128 = 0, 1, 2, 3, 4
@@ -108,7 +108,8 @@ class ServeRecord(C.Structure):
     _fields_ = [("id", C.c_uint64), ("arrival_s", C.c_double), ("admit_s", C.c_double), ("start_s", C.c_double),
                 ("done_s", C.c_double), ("build_rows", C.c_uint64), ("probe_rows", C.c_uint64), ("output_rows", C.c_uint64),
                 ("footprint_bytes", C.c_uint64), ("fingerprint", C.c_uint64 * 3), ("batch_size", C.c_uint32), ("slot", C.c_uint32),
-                ("status", C.c_int32), ("job_peak_bytes", C.c_uint64)]
+                ("status", C.c_int32), ("job_peak_bytes", C.c_uint64), ("gen_s", C.c_double), ("call_s", C.c_double),
+                ("device_ms", C.c_double)]
 
 
 _lib = None
@@ -684,7 +685,8 @@ class Server:
         return [{"id": r.id, "arrival_s": r.arrival_s, "admit_s": r.admit_s, "start_s": r.start_s, "done_s": r.done_s,
                  "build_rows": r.build_rows, "probe_rows": r.probe_rows, "output_rows": r.output_rows,
                  "footprint_bytes": r.footprint_bytes, "fingerprint": tuple(r.fingerprint), "batch_size": r.batch_size,
-                 "slot": r.slot, "status": r.status, "job_peak_bytes": r.job_peak_bytes} for r in arr[:n]]
+                 "slot": r.slot, "status": r.status, "job_peak_bytes": r.job_peak_bytes, "gen_s": r.gen_s, "call_s": r.call_s,
+                 "device_ms": r.device_ms} for r in arr[:n]]
 
     def close(self):
         if self.ptr:

@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol(lib):
 
 
 def test_abi_version(lib):
-    assert lib.phj_abi_version() == P.ABI_VERSION == 2
+    assert lib.phj_abi_version() == P.ABI_VERSION == 3
 
 
 @pytest.mark.parametrize("parts,passes,want", [
@@ -80,7 +80,7 @@ def test_serve_footprint_estimate(lib):
     inputs = 100_000 * 16 + 1_000_000 * 12
     table = cells * 16 + 100_000 * 8
     out = 1_000_000 * (16 + 12 - 8)
-    assert P.serve_footprint(b, p, batched=True) == inputs + table + 1_000_000 * 4 + out
+    assert P.serve_footprint(b, p, batched=True) == inputs + table + 100_000 * 16 + 1_000_000 * 12 + out
     assert P.serve_footprint(b, p, batched=False) == inputs + table + 2 * 100_000 * 16 + 1_000_000 * 12 + 1_000_000 * 4 + out
 
 
@@ -150,5 +150,5 @@ def test_plain_c_caller_links_and_calls_the_library(lib, tmp_path):
                     os.path.join(ROOT, "tests", "cpp", "c_abi_main.c"), "-L", so_dir, "-lphj_gpu", f"-Wl,-rpath,{so_dir}", "-o", exe],
                    check=True)
     out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()
-    assert out[:7] == ["abi", "2", "radix", "0", "2", "8", "8"]
+    assert out[:7] == ["abi", "3", "radix", "0", "2", "8", "8"]
     assert out[7] == "ctx" and int(out[8]) in (0, 6)  # PHJ_OK on a GPU machine, PHJ_ERR_NO_DEVICE without one

@@ -85,6 +85,26 @@ def test_batch_multi_match_and_wide_payloads(ctx):
         t.free()
 
 
+def test_batch_of_medium_joins_equals_the_oracle(ctx):
+    """Medium joins in one batch: 5M build rows (partitions of about 2,400
+    rows, built and probed in two pieces each), 2M and 300K build rows, each
+    equal to the oracle's fingerprint."""
+    sizes = [(5_000_000, 20_000_000, 900), (2_000_000, 8_000_000, 500), (300_000, 9_000_000, 100)]
+    specs = [request(50 + i, B, Pn, m, [P.U64, P.U32], [P.U32, P.U64]) for i, (B, Pn, m) in enumerate(sizes)]
+    hosts = [host_sides(b, p) for b, p in specs]
+    tbs = [ctx.upload(hb) for hb, _ in hosts]
+    tps = [ctx.upload(hp) for _, hp in hosts]
+    try:
+        outs, res = ctx.run_batch(tbs, tps)
+        assert res.n_joins == 3
+        for (hb, hp), o in zip(hosts, outs):
+            assert tuple(o.fingerprint()) == O.join_fingerprint(hb, hp)
+            o.free()
+    finally:
+        for t in tbs + tps:
+            t.free()
+
+
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 def test_served_results_equal_alone(ctx, mode):
     reqs = mix()
