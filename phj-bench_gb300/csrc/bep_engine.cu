@@ -92,7 +92,9 @@ struct EngineCtl
     int more_input;           // some group still has input (decided at each wave's barrier)
     int pool_low;             // a group found too few free blocks for its tile this wave
     int forced_last;          // the previous E was a drain forced by a low pool
+    int any_dup;              // some leaf built so far has a repeated key
     unsigned long long forced_drains;
+    unsigned long long wave_s_max, ns_s_crit; // the slowest group's S time this wave; summed over waves
 };
 
 struct EngineArgs
@@ -775,6 +777,8 @@ __device__ void build_claimed(const EngineArgs & a)
             if (lane == 0)
             {
                 a.meta[L].dup = dup ? 1 : 0;
+                if (dup)
+                    atomicExch(&a.ctl->any_dup, 1);
                 __threadfence();
                 atomicExch(a.state + L, dup ? kBuiltDup : kBuilt);
                 atomicAdd(&a.ctl->tables_built, 1ull);
@@ -806,46 +810,76 @@ __device__ uint32_t lower_bound_warp(const EngineArgs & a, const uint8_t * B, ui
     return lo + __popc(__ballot_sync(0xffffffffu, below));
 }
 
-// Match count and head build row of one probe key.  The leaf's table was
-// built during this launch, so cells, chain and state are read through L2.
-__device__ __forceinline__ uint32_t lookup(const EngineArgs & a, uint64_t key, uint32_t & head)
+// A lookup in two halves, so that several rows' first loads are in flight
+// at once: probe_issue loads the aligned pair of cells the key's probe
+// starts at (through L2: the leaf's table was built during this launch);
+// probe_finish compares, follows the table past the pair when needed, and
+// returns the match count (the next-chain's length when some leaf table has
+// a repeated key) and the head build row.
+__device__ __forceinline__ const Cell * leaf_table(const EngineArgs & a, uint64_t h, uint64_t & cap)
 {
-    const uint64_t h = int_hash64(key);
     const uint32_t L = (uint32_t)(h >> (64u - a.total_bits));
-    const Cell * tab;
-    uint64_t cap;
     if (a.ulog >= 0)
     {
         cap = 1ull << a.ulog;
-        tab = a.cells + ((uint64_t)L << a.ulog);
+        return a.cells + ((uint64_t)L << a.ulog);
     }
-    else
+    const ulonglong2 m = __ldcg(reinterpret_cast<const ulonglong2 *>(a.meta + L));
+    cap = ((m.y >> 40) & 0xffu) ? 1ull << ((uint32_t)(m.y >> 32) & 0xffu) : 0ull;
+    return a.cells + m.x;
+}
+
+__device__ __forceinline__ CellPair probe_issue(const EngineArgs & a, uint64_t h)
+{
+    uint64_t cap;
+    const Cell * tab = leaf_table(a, h, cap);
+    if (cap == 0)
     {
-        const ulonglong2 m = __ldcg(reinterpret_cast<const ulonglong2 *>(a.meta + L));
-        if (!((m.y >> 40) & 0xffu))
-            return 0;
-        cap = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
-        tab = a.cells + m.x;
+        CellPair none;
+        none.a = make_ulonglong2(0ull, INVALID_REF);
+        none.b = none.a;
+        return none;
     }
-    const uint32_t st = __ldcg(a.state + L); // beside the first cell load
-    const uint64_t mask = cap - 1;
-    uint64_t pos = probe_start(h, cap), r = INVALID_REF;
-    for (uint64_t step = 0; step < cap; ++step)
+    return load_pair<true>(tab + probe_start(h, cap));
+}
+
+__device__ __forceinline__ uint32_t probe_finish(const EngineArgs & a, uint64_t key, uint64_t h, const CellPair & pr, bool chains, uint32_t & head)
+{
+    uint64_t r = INVALID_REF;
+    if (ref_valid(pr.a.y))
     {
-        const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + pos));
-        if (!ref_valid(c.y))
-            break;
-        if (c.x == key)
+        if (pr.a.x == key)
+            r = pr.a.y;
+        else if (ref_valid(pr.b.y))
         {
-            r = c.y;
-            break;
+            if (pr.b.x == key)
+                r = pr.b.y;
+            else
+            {
+                // past the pair: follow the table
+                uint64_t cap;
+                const Cell * tab = leaf_table(a, h, cap);
+                const uint64_t mask = cap - 1;
+                uint64_t pos = (probe_start(h, cap) + 2) & mask;
+                for (uint64_t step = 2; step < cap; ++step)
+                {
+                    const ulonglong2 c = __ldcg(reinterpret_cast<const ulonglong2 *>(tab + pos));
+                    if (!ref_valid(c.y))
+                        break;
+                    if (c.x == key)
+                    {
+                        r = c.y;
+                        break;
+                    }
+                    pos = (pos + 1) & mask;
+                }
+            }
         }
-        pos = (pos + 1) & mask;
     }
     if (!ref_valid(r))
         return 0;
     head = ref_row(r);
-    if (st != kBuiltDup)
+    if (!chains)
         return 1;
     uint32_t c = 1;
     for (unsigned long long x = __ldcg(reinterpret_cast<const unsigned long long *>(a.next) + head); ref_valid(x);
@@ -858,8 +892,8 @@ __device__ __forceinline__ uint32_t lookup(const EngineArgs & a, uint64_t key, u
 // matches, 256 rows a step with one reservation of output rows; a step's
 // output rows are placed round by round so each store instruction writes
 // consecutive rows.
-constexpr uint32_t kWarpRows = 8; // rows per lane per step
-__device__ void probe_rows_warp(const EngineArgs & a, const uint8_t * B, uint32_t r0, uint32_t r1, uint32_t lane)
+constexpr uint32_t kWarpRows = 4; // rows per lane per step
+__device__ void probe_rows_warp(const EngineArgs & a, const uint8_t * B, uint32_t r0, uint32_t r1, uint32_t lane, bool chains)
 {
     const unsigned long long * keys = reinterpret_cast<const unsigned long long *>(B);
     for (uint32_t base = r0; base < r1; base += 32 * kWarpRows)
@@ -872,12 +906,25 @@ __device__ void probe_rows_warp(const EngineArgs & a, const uint8_t * B, uint32_
             const uint32_t i = base + k * 32 + lane;
             key[k] = i < r1 ? __ldcg(keys + i) : 0ull;
         }
+        // four first loads in flight, then their comparisons
 #pragma unroll
-        for (uint32_t k = 0; k < kWarpRows; ++k)
+        for (uint32_t g = 0; g < kWarpRows; g += 4)
         {
-            const uint32_t i = base + k * 32 + lane;
-            head[k] = 0;
-            cnt[k] = i < r1 ? lookup(a, key[k], head[k]) : 0u;
+            CellPair pr[4];
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u)
+            {
+                const uint32_t i = base + (g + u) * 32 + lane;
+                if (i < r1)
+                    pr[u] = probe_issue(a, int_hash64(key[g + u]));
+            }
+#pragma unroll
+            for (uint32_t u = 0; u < 4; ++u)
+            {
+                const uint32_t i = base + (g + u) * 32 + lane;
+                head[g + u] = 0;
+                cnt[g + u] = i < r1 ? probe_finish(a, key[g + u], int_hash64(key[g + u]), pr[u], chains, head[g + u]) : 0u;
+            }
         }
         // placement: a warp scan per round, rounds one after another
         uint32_t rel[kWarpRows], total = 0;
@@ -957,8 +1004,11 @@ __device__ bool evict_phase(const EngineArgs & a, const Smem & sm, uint32_t & ge
                 a.leaf_rows[L] = 0;
                 rows += r;
                 ++ev;
-                if (ld_acquire_u32(a.state + L) < kBuilt)
+                const uint32_t st = ld_acquire_u32(a.state + L);
+                if (st < kBuilt)
                     a.build_queue[atomicAdd(&a.ctl->build_n, 1u)] = L;
+                else if (st == kBuiltDup)
+                    atomicExch(&a.ctl->any_dup, 1); // built by an earlier run over these tables
             }
             atomicExch(a.leaf_lock + L, 0u);
         }
@@ -1024,6 +1074,7 @@ __device__ bool evict_phase(const EngineArgs & a, const Smem & sm, uint32_t & ge
     {
         constexpr uint32_t kPart = 1024;
         const uint32_t lane = threadIdx.x & 31;
+        const bool chains = vload(&a.ctl->any_dup) != 0; // some leaf table has a repeated key
         const uint32_t parts = (1u << a.page_log2) > kPart ? (1u << a.page_log2) / kPart : 1u;
         const uint32_t part_rows = (1u << a.page_log2) / parts;
         const uint64_t n_items = (uint64_t)vload(&a.ctl->work_n) * parts;
@@ -1060,7 +1111,7 @@ __device__ bool evict_phase(const EngineArgs & a, const Smem & sm, uint32_t & ge
                 rb = rb < c1r ? rb : c1r;
                 if (rb <= ra)
                     continue;
-                probe_rows_warp(a, B, ra, rb, lane);
+                probe_rows_warp(a, B, ra, rb, lane, chains);
                 done += rb - ra;
             }
             if (lane == 0 && done)
@@ -1110,6 +1161,8 @@ struct WaveEnd
             c->forced_drains += 1;
         c->pool_low = 0;
         c->evict_now = low ? 2 : (r > 0 && r * a->rb >= a->leaf_high ? 1 : 0);
+        c->ns_s_crit += c->wave_s_max;
+        c->wave_s_max = 0;
         c->more_input = vload(&c->groups_done) < gridDim.x;
     }
 };
@@ -1202,8 +1255,13 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
             refine_down_to(a, sm, g, unref_bytes, 0); // stalled: everything it holds goes to the drain
         else if (unref_bytes >= a.unref_high)
             refine_down_to(a, sm, g, unref_bytes, a.unref_low);
-        if (g == 0 && threadIdx.x == 0)
-            a.ctl->ns_shuffle += now_ns() - t0;
+        if (threadIdx.x == 0)
+        {
+            const unsigned long long dt = now_ns() - t0;
+            if (g == 0)
+                a.ctl->ns_shuffle += dt;
+            atomicMax(&a.ctl->wave_s_max, dt);
+        }
         // the last group to arrive records the peak and decides the E
         if (!grid_sync(a, gen, WaveEnd{&a}))
             return;
@@ -1387,8 +1445,11 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     res.ms_probe = c.ns_probe * 1e-6;
     res.pool_bytes = (uint64_t)a.n_blocks * a.block_bytes;
     if (std::getenv("PHJ_DEBUG"))
-        std::fprintf(stderr, "[phj] bep_engine rows: scattered %llu refined %llu claimed %llu probed %llu out %llu; E phases %llu, err %d\n",
-                     c.rows_scattered, c.rows_refined, c.rows_claimed, c.rows_probed, c.out_rows, c.evict_phases, e);
+        std::fprintf(stderr,
+                     "[phj] bep_engine rows: scattered %llu refined %llu claimed %llu probed %llu out %llu; E phases %llu (forced %llu), "
+                     "S critical path %.3f ms, err %d\n",
+                     c.rows_scattered, c.rows_refined, c.rows_claimed, c.rows_probed, c.out_rows, c.evict_phases, c.forced_drains, c.ns_s_crit * 1e-6,
+                     e);
     res.groups = G;
     return res;
 }
