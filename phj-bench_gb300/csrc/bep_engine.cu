@@ -1432,6 +1432,21 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     EngineCtl c{};
     int e = 0;
     read_small(ctx, {{&c, a.ctl, sizeof(c)}, {&e, ctx->d_err, sizeof(e)}});
+    // the launch's algorithmic bytes, as the join's: every probe row read
+    // once, every output row written once
+    {
+        uint64_t orow = 8;
+        for (uint32_t c2 = 0; c2 < in.build.n; ++c2)
+            orow += in.build.width[c2];
+        for (uint32_t c2 = 0; c2 < in.probe.n; ++c2)
+            orow += in.probe.width[c2];
+        for (size_t i = ctx->records.size(); i-- > 0;)
+            if (ctx->records[i].name == "bep_engine")
+            {
+                ctx->records[i].bytes = in.probe_rows * rb + std::min<uint64_t>(c.out_rows, a.out_cap) * orow;
+                break;
+            }
+    }
     res.err = e;
     res.out_rows = c.out_rows;
     res.evictions = c.evictions;
