@@ -95,7 +95,10 @@ struct EngineCtl
     int any_dup;              // some leaf built so far has a repeated key
     unsigned long long forced_drains;
     unsigned long long wave_s_max, ns_s_crit; // the slowest group's S time this wave; summed over waves
+    unsigned long long ns_refine0, tiles0, blocks0; // group 0: time refining, tiles scattered, blocks refined
 };
+
+static_assert(sizeof(EngineCtl) + 8 <= kSmallReadBytes, "the control block and the error word are read back in one small read");
 
 struct EngineArgs
 {
@@ -308,6 +311,7 @@ struct Smem
     uint32_t * clen;  // buckets: blocks in each chain
     uint32_t * urows; // buckets: unrefined rows per bucket
     uint32_t * acc;   // leaves per bucket: rows a refine adds to each leaf
+    uint32_t * bcache; // the group's free blocks: 2 x buckets + 2 x kRefill entries
     uint32_t * ws;    // scan scratch (kENT / 32 words)
     uint32_t * scal;  // scalars (32 words, 8-byte aligned)
 };
@@ -316,6 +320,7 @@ struct Smem
 // S: scatter `n` (<= page) input rows from `r0` into the group's chains.
 // ---------------------------------------------------------------------------
 constexpr int kTileDone = 0, kTileNoRoom = 1, kTileFailed = 2;
+constexpr uint32_t kRefill = 64; // free blocks a group takes beyond its need
 
 // Returns kTileDone, kTileNoRoom (too few free blocks: nothing done) or
 // kTileFailed (the grid is ending).  sm.bins[0, buckets) is zero on entry
@@ -362,26 +367,33 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
     __syncthreads();
     const uint32_t tot = scan_bins(sm.boff, P1, sm.ws);
     const uint32_t nb_total = tot & 0xFFFFu;
+    // blocks come from the group's cache of free blocks (sm.bcache, its
+    // length in scal[16]), refilled from the pool's stack kRefill blocks
+    // beyond the need at a time, so the groups rarely meet on the stack
     if (threadIdx.x == 0)
     {
         sm.scal[0] = 0;
         sm.scal[1] = 0;
-        if (nb_total)
+        sm.scal[2] = 0;
+        const uint32_t have = sm.scal[16];
+        if (nb_total > have)
         {
-            // take nb_total blocks off the stack, or none when it holds fewer
+            const uint32_t need = nb_total - have, want = need + kRefill;
             unsigned long long * top = reinterpret_cast<unsigned long long *>(&a.ctl->free_top);
             long long cur = (long long)vload(top);
             for (;;)
             {
-                if (cur < (long long)nb_total)
+                const long long take = cur >= (long long)want ? (long long)want : (cur >= (long long)need ? cur : 0);
+                if (take == 0)
                 {
-                    sm.scal[0] = 2;
+                    sm.scal[0] = 2; // too few free blocks
                     break;
                 }
-                const long long seen = (long long)atomicCAS(top, (unsigned long long)cur, (unsigned long long)(cur - (long long)nb_total));
+                const long long seen = (long long)atomicCAS(top, (unsigned long long)cur, (unsigned long long)(cur - take));
                 if (seen == cur)
                 {
-                    sm.scal[1] = (uint32_t)(cur - (long long)nb_total);
+                    sm.scal[1] = (uint32_t)(cur - take);
+                    sm.scal[2] = (uint32_t)take;
                     break;
                 }
                 cur = seen;
@@ -396,6 +408,17 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
         __syncthreads();
         return kTileNoRoom;
     }
+    if (sm.scal[2])
+    {
+        const uint32_t have = sm.scal[16];
+        for (uint32_t i = threadIdx.x; i < sm.scal[2]; i += kENT)
+            sm.bcache[have + i] = __ldcg(a.free_stack + sm.scal[1] + i);
+        __syncthreads();
+        if (threadIdx.x == 0)
+            sm.scal[16] = have + sm.scal[2];
+        __syncthreads();
+    }
+    const uint32_t cache_base = sm.scal[16] - nb_total; // this tile's blocks: bcache[cache_base, +nb_total)
     // new blocks onto the chains; the cursors of the sorted tile
     for (uint32_t p = threadIdx.x; p < P1; p += kENT)
     {
@@ -413,11 +436,13 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
         }
         uint32_t * ch = a.chain + ((uint64_t)g * P1 + p) * a.maxb;
         for (uint32_t j = 0; j < nb; ++j)
-            ch[len + j] = __ldcg(a.free_stack + sm.scal[1] + nb0 + j);
+            ch[len + j] = sm.bcache[cache_base + nb0 + j];
     }
     __syncthreads();
     if (sm.scal[0])
         return kTileFailed;
+    if (threadIdx.x == 0)
+        sm.scal[16] = cache_base; // read by no thread before the next tile's syncs
     // the stage row of every sorted position
     for (uint32_t i = threadIdx.x; i < n; i += kENT)
         sm.src[atomicAdd(&sm.bins[sm.perm[i]], 1u)] = (uint16_t)i;
@@ -524,6 +549,8 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
             a.blk_rem[blk] = n;
             a.blk_bucket[blk] = p;
             a.blk_c0[blk] = vload(&a.ctl->cursor); // the cursor stands still outside E
+            if (g == 0)
+                a.ctl->blocks0 += 1;
             a.blk_state[blk] = p;
         }
         __syncthreads();
@@ -1198,6 +1225,8 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
         p += ((uint64_t)P1 * 4 + 15) & ~15ull;
         sm.acc = reinterpret_cast<uint32_t *>(p);
         p += ((uint64_t)LB * 4 + 15) & ~15ull;
+        sm.bcache = reinterpret_cast<uint32_t *>(p);
+        p += ((uint64_t)(2 * P1 + 2 * kRefill) * 4 + 15) & ~15ull;
         sm.ws = reinterpret_cast<uint32_t *>(p);
         p += (kENT / 32) * 4;
         sm.scal = reinterpret_cast<uint32_t *>(p);
@@ -1243,7 +1272,11 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
             pos += n;
             unref_bytes += (uint64_t)n * a.rb;
             if (threadIdx.x == 0)
+            {
                 atomicAdd(&a.ctl->rows_scattered, (unsigned long long)n);
+                if (g == 0)
+                    a.ctl->tiles0 += 1;
+            }
         }
         if (pos >= hi && !counted)
         {
@@ -1251,10 +1284,13 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
             if (threadIdx.x == 0)
                 atomicAdd(&a.ctl->groups_done, 1u);
         }
+        const uint64_t t_ref = now_ns();
         if (pos < end)
             refine_down_to(a, sm, g, unref_bytes, 0); // stalled: everything it holds goes to the drain
         else if (unref_bytes >= a.unref_high)
             refine_down_to(a, sm, g, unref_bytes, a.unref_low);
+        if (g == 0 && threadIdx.x == 0)
+            a.ctl->ns_refine0 += now_ns() - t_ref;
         if (threadIdx.x == 0)
         {
             const unsigned long long dt = now_ns() - t0;
@@ -1371,7 +1407,7 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     const uint64_t leaf_rows_max = a.leaf_high / rb + G * (high_rows + a.tile_rows);
     const uint64_t by_budget = unref_blocks + ceil_div(leaf_rows_max, page) + 2 * G * P1;
     const uint64_t by_input = ceil_div(in.probe_rows + in.probe_rows / 4, page) + 2 * G * (P1 + 2) + G * ceil_div(a.tile_rows, page);
-    const uint64_t n_blocks = std::max<uint64_t>(std::min(by_budget, by_input), 2 * unref_blocks);
+    const uint64_t n_blocks = std::max<uint64_t>(std::min(by_budget, by_input), 2 * unref_blocks) + (uint64_t)G * (kRefill + 8);
     if (n_blocks >= (1ull << 31))
         throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP): the probe side needs more blocks than the device budget engine indexes");
     a.n_blocks = (uint32_t)n_blocks;
@@ -1411,7 +1447,7 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     const uint64_t stage = std::max<uint64_t>(page * rb, (uint64_t)a.smem_cells * sizeof(Cell));
     const uint64_t nbins = std::max(std::max(P1, LB), page);
     const size_t smem = ((stage + 15) & ~15ull) + 2 * ((page * 2 + 15) & ~15ull) + ((nbins * 4 + 15) & ~15ull) + 5 * ((P1 * 4 + 15) & ~15ull) +
-                        ((LB * 4 + 15) & ~15ull) + (kENT / 32) * 4 + 32 * 4;
+                        ((LB * 4 + 15) & ~15ull) + (((2 * P1 + 2 * kRefill) * 4 + 15) & ~15ull) + (kENT / 32) * 4 + 32 * 4;
     if (smem + 1024 > (size_t)ctx->smem_optin)
         throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP): the device budget engine's shared memory does not fit this configuration");
     PHJ_CUDA(cudaFuncSetAttribute(k_bep_engine, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -1462,9 +1498,9 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
     if (std::getenv("PHJ_DEBUG"))
         std::fprintf(stderr,
                      "[phj] bep_engine rows: scattered %llu refined %llu claimed %llu probed %llu out %llu; E phases %llu (forced %llu), "
-                     "S critical path %.3f ms, err %d\n",
+                     "S critical path %.3f ms (group 0: %llu tiles, %llu blocks refined in %.3f ms), err %d\n",
                      c.rows_scattered, c.rows_refined, c.rows_claimed, c.rows_probed, c.out_rows, c.evict_phases, c.forced_drains, c.ns_s_crit * 1e-6,
-                     e);
+                     c.tiles0, c.blocks0, c.ns_refine0 * 1e-6, e);
     res.groups = G;
     return res;
 }

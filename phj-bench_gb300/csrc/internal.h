@@ -158,7 +158,7 @@ struct SmallRead
     uint32_t bytes;
 };
 constexpr uint32_t kMaxSmallReads = 8;
-constexpr uint32_t kSmallReadBytes = 256;
+constexpr uint32_t kSmallReadBytes = 512;
 void read_small(phj_ctx * ctx, std::initializer_list<SmallRead> reads);
 void reset_accounting(phj_ctx * ctx);
 
