@@ -299,6 +299,43 @@ __device__ __forceinline__ void copy_row(const EngineArgs & a, uint8_t * dst, ui
     }
 }
 
+// Column c of rows i0 + u * kENT + threadIdx.x (u < 4, below n) from `src`
+// (row r0 + i) into the stage column `dst`: the four loads are issued
+// before any store.  kL2: the source was written during this launch (read
+// through L2).
+template <class T, bool kL2>
+__device__ __forceinline__ void stage4(T * dst, const T * src, uint64_t r0, uint32_t i0, uint32_t n)
+{
+    T v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+    {
+        const uint32_t i = i0 + u * kENT + threadIdx.x;
+        if (i < n)
+            v[u] = kL2 ? __ldcg(src + r0 + i) : src[r0 + i];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u)
+    {
+        const uint32_t i = i0 + u * kENT + threadIdx.x;
+        if (i < n)
+            dst[i] = v[u];
+    }
+}
+
+template <bool kL2>
+__device__ __forceinline__ void stage4_column(void * dst, const void * src, uint64_t r0, uint32_t i0, uint32_t n, uint32_t w)
+{
+    switch (w)
+    {
+        case 1: stage4<unsigned char, kL2>(static_cast<unsigned char *>(dst), static_cast<const unsigned char *>(src), r0, i0, n); break;
+        case 2: stage4<unsigned short, kL2>(static_cast<unsigned short *>(dst), static_cast<const unsigned short *>(src), r0, i0, n); break;
+        case 4: stage4<unsigned int, kL2>(static_cast<unsigned int *>(dst), static_cast<const unsigned int *>(src), r0, i0, n); break;
+        case 8: stage4<unsigned long long, kL2>(static_cast<unsigned long long *>(dst), static_cast<const unsigned long long *>(src), r0, i0, n); break;
+        default: stage4<uint4, kL2>(static_cast<uint4 *>(dst), static_cast<const uint4 *>(src), r0, i0, n); break;
+    }
+}
+
 struct Smem
 {
     uint8_t * stage;  // page rows in the block layout; the leaf builds' cells
@@ -340,6 +377,8 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
             const uint32_t i = i0 + u * kENT + threadIdx.x;
             k[u] = i < n ? a.pin.keys[r0 + i] : 0ull;
         }
+        for (uint32_t c = 0; c < a.pin.n; ++c)
+            stage4_column<false>(sm.stage + a.col_off[c], a.pin.col[c], r0, i0, n, a.pin.width[c]);
 #pragma unroll
         for (int u = 0; u < 4; ++u)
         {
@@ -347,8 +386,6 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
             if (i < n)
             {
                 reinterpret_cast<uint64_t *>(sm.stage)[i] = k[u];
-                for (uint32_t c = 0; c < a.pin.n; ++c)
-                    copy_elem(sm.stage + a.col_off[c], i, a.pin.col[c], r0 + i, a.pin.width[c]);
                 const uint32_t p = (uint32_t)(int_hash64(k[u]) >> (64u - a.b1));
                 sm.perm[i] = (uint16_t)p;
                 atomicAdd(&sm.bins[p], 1u);
@@ -507,6 +544,8 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
                 const uint32_t i = i0 + u * kENT + threadIdx.x;
                 k[u] = i < n ? __ldcg(reinterpret_cast<const unsigned long long *>(B) + i) : 0ull;
             }
+            for (uint32_t c = 0; c < a.pin.n; ++c)
+                stage4_column<true>(sm.stage + a.col_off[c], B + a.col_off[c], 0, i0, n, a.pin.width[c]);
 #pragma unroll
             for (int u = 0; u < 4; ++u)
             {
@@ -514,8 +553,6 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
                 if (i < n)
                 {
                     reinterpret_cast<uint64_t *>(sm.stage)[i] = k[u];
-                    for (uint32_t c = 0; c < a.pin.n; ++c)
-                        copy_elem_cg(sm.stage + a.col_off[c], i, B + a.col_off[c], i, a.pin.width[c]);
                     const uint32_t l = (uint32_t)(int_hash64(k[u]) >> shift) & (LB - 1u);
                     sm.perm[i] = (uint16_t)l;
                     atomicAdd(&sm.bins[l], 1u);
