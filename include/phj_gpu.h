@@ -187,6 +187,10 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        batches take the configuration's first pass;
  *   "test_stuck_leaf": test hook, -1 (default) off; >= 0 leaves that PHJ/BEP
  *        leaf BUILDING before the probe, so its waits run out;
+ *   "test_engine_stall_wave": test hook, -1 (default) off; >= 0 makes one
+ *        CTA group of the PHJ (BEP) budget engine hold back from that
+ *        wave's grid barrier until the others' bounded wait runs out, so
+ *        the run fails with PHJ_ERR_DEVICE_TIMEOUT;
  *   "test_fail_build": test hook, 0 (default) off; 1 makes the host-buffer
  *        joins return PHJ_ERR_CUDA right after the build shuffle, with
  *        their uploads still queued. */

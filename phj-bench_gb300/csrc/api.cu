@@ -1738,6 +1738,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
         ctx->test_stuck_leaf = value;
+    else if (std::strcmp(name, "test_engine_stall_wave") == 0 && value >= -1 && value < (1ll << 31))
+        ctx->test_engine_stall_wave = value;
     else if (std::strcmp(name, "test_fail_build") == 0 && (value == 0 || value == 1))
         ctx->test_fail_build = (int)value;
     else
@@ -1773,6 +1775,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)
         *value = ctx->test_stuck_leaf;
+    else if (std::strcmp(name, "test_engine_stall_wave") == 0)
+        *value = ctx->test_engine_stall_wave;
     else if (std::strcmp(name, "test_fail_build") == 0)
         *value = ctx->test_fail_build;
     else if (std::strcmp(name, "device") == 0)

@@ -151,6 +151,7 @@ struct EngineArgs
     void * out_r[kMaxCols];
     uint64_t out_cap;
     uint64_t wait_limit_ns;
+    uint32_t test_stall_wave; // test hook: group 0 holds back from this wave's barrier (kNone: off)
     EngineCtl * ctl;
     int * err;
 };
@@ -1284,7 +1285,7 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
     uint64_t pos = lo, unref_bytes = 0;
     uint32_t gen = 0;
     bool counted = false; // this group is counted in groups_done
-    for (;;)
+    for (uint32_t wave = 0;; ++wave)
     {
         // -------- S: this wave's tile of the slice, then the refine trigger --------
         const uint64_t t0 = now_ns();
@@ -1334,6 +1335,14 @@ __global__ void __launch_bounds__(kENT, 1) k_bep_engine(const __grid_constant__ 
             if (g == 0)
                 a.ctl->ns_shuffle += dt;
             atomicMax(&a.ctl->wave_s_max, dt);
+        }
+        if (wave == a.test_stall_wave && g == 0 && threadIdx.x == 0)
+        {
+            // test hook: this group holds back from the barrier until the
+            // others' bounded wait runs out and ends the grid (bounded too)
+            const uint64_t ts = now_ns();
+            while (!aborted(a) && now_ns() - ts < 4 * a.wait_limit_ns)
+                __nanosleep(1000);
         }
         // the last group to arrive records the peak and decides the E
         if (!grid_sync(a, gen, WaveEnd{&a}))
@@ -1472,6 +1481,7 @@ BepEngineResult bep_engine_run(phj_ctx * ctx, Scratch & s, const BepEngineInput 
         a.out_r[c] = out->rcol[c];
     a.out_cap = out->cap;
     a.wait_limit_ns = (uint64_t)ctx->wait_limit_ms * 1000000ull;
+    a.test_stall_wave = ctx->test_engine_stall_wave >= 0 ? (uint32_t)ctx->test_engine_stall_wave : kNone;
     a.ctl = s.get<EngineCtl>(1);
     a.err = ctx->d_err;
     PHJ_CUDA(cudaMemsetAsync(a.ctl, 0, sizeof(EngineCtl), ctx->stream));

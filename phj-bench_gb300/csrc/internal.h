@@ -112,6 +112,7 @@ struct phj_ctx
     uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
+    int64_t test_engine_stall_wave = -1; // test hook: a BEP engine group holds back from this wave's barrier
     int test_fail_build = 0;      // test hook: host-buffer joins fail on the host after the build shuffle
     LeafMark leaf_mark;           // consumed by the next first radix pass
 };

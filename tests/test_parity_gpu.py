@@ -278,6 +278,25 @@ def test_bep_stuck_leaf_times_out_and_context_recovers(ctx):
     check(b, p, jo, fp)
 
 
+def test_bep_engine_barrier_wait_runs_out_and_context_recovers(ctx):
+    """One CTA group of the budget engine holds back from the first wave's
+    grid barrier (a host-set hook, no fault): the other groups' bounded
+    wait runs out, the grid ends, the run fails with PHJ_ERR_DEVICE_TIMEOUT,
+    and the context runs the next join bit-exactly."""
+    b, p = cases.make("c2_mini")
+    ctx.set_int("wait_limit_ms", 50)
+    ctx.set_int("test_engine_stall_wave", 0)
+    try:
+        with pytest.raises(P.PhjError) as e:
+            run(ctx, "phj", b, p, [4, 4])
+        assert e.value.status == P.ERR_DEVICE_TIMEOUT
+    finally:
+        ctx.set_int("test_engine_stall_wave", -1)
+        ctx.set_int("wait_limit_ms", 1000)
+    jo, fp, _ = run(ctx, "phj", b, p, [4, 4])
+    check(b, p, jo, fp)
+
+
 def test_bep_invalid_budget_and_too_many_leaves(ctx):
     b, p = cases.make("c2_mini")
     tb, tp = ctx.upload(b), ctx.upload(p)
