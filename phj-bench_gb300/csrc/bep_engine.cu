@@ -280,24 +280,13 @@ __device__ __forceinline__ uint8_t * block_ptr(const EngineArgs & a, uint32_t bl
     return a.pool + (uint64_t)blk * a.block_bytes;
 }
 
-// Copies row `src_i` of a column-major tile (keys at 0, payload c at
-// col_off[c]) to row `dst_i` of another tile of the same layout;
-// kFromPool: the source is a pool block (read through L2).
-template <bool kFromPool>
+// Copies row `src_i` of a column-major tile in shared memory (keys at 0,
+// payload c at col_off[c]) to row `dst_i` of a block of the same layout.
 __device__ __forceinline__ void copy_row(const EngineArgs & a, uint8_t * dst, uint32_t dst_i, const uint8_t * src, uint32_t src_i)
 {
-    if (kFromPool)
-    {
-        reinterpret_cast<unsigned long long *>(dst)[dst_i] = __ldcg(reinterpret_cast<const unsigned long long *>(src) + src_i);
-        for (uint32_t c = 0; c < a.pin.n; ++c)
-            copy_elem_cg(dst + a.col_off[c], dst_i, src + a.col_off[c], src_i, a.pin.width[c]);
-    }
-    else
-    {
-        reinterpret_cast<uint64_t *>(dst)[dst_i] = reinterpret_cast<const uint64_t *>(src)[src_i];
-        for (uint32_t c = 0; c < a.pin.n; ++c)
-            copy_elem(dst + a.col_off[c], dst_i, src + a.col_off[c], src_i, a.pin.width[c]);
-    }
+    reinterpret_cast<uint64_t *>(dst)[dst_i] = reinterpret_cast<const uint64_t *>(src)[src_i];
+    for (uint32_t c = 0; c < a.pin.n; ++c)
+        copy_elem(dst + a.col_off[c], dst_i, src + a.col_off[c], src_i, a.pin.width[c]);
 }
 
 // Column c of rows i0 + u * kENT + threadIdx.x (u < 4, below n) from `src`
@@ -495,7 +484,7 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
         const uint32_t q = sm.fill[p] + (s - (sm.boff[p] >> 16)); // slot counted from the chain's last block
         const uint32_t idx = sm.clen[p] + (q >> a.page_log2) - 1u;
         const uint32_t blk = a.chain[((uint64_t)g * P1 + p) * a.maxb + idx];
-        copy_row<false>(a, block_ptr(a, blk), q & (page - 1), sm.stage, r);
+        copy_row(a, block_ptr(a, blk), q & (page - 1), sm.stage, r);
     }
     __syncthreads();
     for (uint32_t p = threadIdx.x; p < P1; p += kENT)
@@ -576,7 +565,7 @@ __device__ uint32_t refine_bucket(const EngineArgs & a, const Smem & sm, uint32_
             src[sm.perm[i]] = i;
         __syncthreads();
         for (uint32_t s = threadIdx.x; s < n; s += kENT)
-            copy_row<false>(a, B, s, sm.stage, src[s]);
+            copy_row(a, B, s, sm.stage, src[s]);
         if (threadIdx.x == 0)
         {
             // the leaves of its first and last rows: E probes a block that
