@@ -43,8 +43,12 @@
 // retries (claims that found the leaf locked, and waits on a BUILDING leaf).
 //
 // Every wait is bounded: the grid barrier and the BUILDING wait give up
-// after the context's wait limit, set an error code and end the grid; an
-// exhausted block pool ends it with a capacity error.
+// after the context's wait limit, set an error code and end the grid.  A
+// group that finds too few free blocks for its tile refines what it holds
+// and the wave ends in a drain of every leaf (which frees every refined
+// block); a second shortage right after such a drain ends the grid with a
+// capacity error.  Each group takes its free blocks from a cache of its own,
+// refilled from the pool's stack a batch at a time.
 //
 // Pool blocks, control words, per-leaf and per-block state and the lazily
 // built tables are written by one group and read by others during the
