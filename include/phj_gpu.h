@@ -312,13 +312,18 @@ phj_status phj_run_phj_bep_host(phj_ctx *ctx, const phj_block_stream *build, con
                                 phj_bep_result *result);
 
 /* Batching (no counterpart in the reference: it runs one join per call).
- * Runs n independent joins in one set of launches (clear, build, lookup,
- * scan, project, each over all n joins through a device work list of
- * (join, tile) items); outs[j] receives join j's output, the same multiset
- * of rows as a single-join entry point gives for that pair.  Meant for small
- * and medium joins, whose single launches would not fill the device; a
- * batch whose joins have 2^32 output rows or more in all returns
- * PHJ_ERR_CAPACITY (run large joins on their own). */
+ * Runs n independent joins together: every join's build and probe sides are
+ * radix-partitioned by the same launches (histogram, scan, scatter over
+ * (join, tile) items, about 1024 build rows a partition), then ONE
+ * persistent launch whose CTAs take (join, partition) items from a device
+ * queue builds each partition's table in shared memory, probes its rows and
+ * projects the matches; outs[j] receives join j's output, the same multiset
+ * of rows as a single-join entry point gives for that pair, in no fixed
+ * order.  A join is given one output row per probe row; one that needs more
+ * (repeated build keys) is counted, then run again on its own.  Meant for
+ * small and medium joins, whose single launches would not fill the device;
+ * fewer than 2^31 build rows and 2^31 probe rows a join, and fewer than
+ * 2^32 on each side in all (PHJ_ERR_UNSUPPORTED otherwise). */
 phj_status phj_batch_run(phj_ctx *ctx, uint32_t n, const phj_table *const *builds, const phj_table *const *probes,
                          phj_output **outs, phj_batch_result *result);
 
