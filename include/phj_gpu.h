@@ -179,8 +179,8 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        bep_budget_mib, scatter their slice of the probe side into
  *        first-pass chains, refine at the reference's water marks and
  *        evict leaves round-robin (first pass 1..11 bits with at most 13
- *        bits below it; other configurations take the batch form); 1
- *        budget-sized probe batches;
+ *        bits below it, fewer than 2^32 probe rows; other joins take the
+ *        batch form); 1 budget-sized probe batches;
  *   "probe_pass_bits": bits of the radix pass written out for the probe
  *        side, 1..11; 0 (default): PHJ-PURE chooses them from the build
  *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's

@@ -2070,7 +2070,8 @@ phj_status phj_run_phj_bep(phj_ctx * ctx, const phj_table * build, const phj_tab
             total += b;
         if (total > 20)
             throw Error(PHJ_ERR_UNSUPPORTED, "PHJ (BEP) on the device takes at most 20 radix bits (2^20 leaves)");
-        if (ctx->bep_engine == 0 && bep_engine_supported(bits[0], total))
+        // the engine counts a leaf's and a block's rows in 32 bits
+        if (ctx->bep_engine == 0 && bep_engine_supported(bits[0], total) && probe->rows < (1ull << 32))
             run_phj_bep_engine(ctx, *build, *probe, bits, bep_budget_mib, out, result);
         else
             run_phj_bep(ctx, *build, *probe, bits, bep_budget_mib, out, result);
