@@ -181,6 +181,10 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        evict leaves round-robin (first pass 1..11 bits with at most 13
  *        bits below it, fewer than 2^32 probe rows; other joins take the
  *        batch form); 1 budget-sized probe batches;
+ *   "batch_graph": phj_batch_run's chain; 1 (default) replays it as a
+ *        captured CUDA graph (one timing record, "batch_graph"), 0 launches
+ *        it kernel by kernel at the batch's own sizes (a timing record per
+ *        kernel).  Same output rows;
  *   "probe_pass_bits": bits of the radix pass written out for the probe
  *        side, 1..11; 0 (default): PHJ-PURE chooses them from the build
  *        side's size so one bucket's leaf tables stay in L2, PHJ/BEP's
@@ -323,7 +327,13 @@ phj_status phj_run_phj_bep_host(phj_ctx *ctx, const phj_block_stream *build, con
  * (repeated build keys) is counted, then run again on its own.  Meant for
  * small and medium joins, whose single launches would not fill the device;
  * fewer than 2^31 build rows and 2^31 probe rows a join, and fewer than
- * 2^32 on each side in all (PHJ_ERR_UNSUPPORTED otherwise). */
+ * 2^32 on each side in all (PHJ_ERR_UNSUPPORTED otherwise).  The chain
+ * between the one upload of the batch's descriptors and the one download
+ * of its row counts reads nothing back to the host; it is captured into a
+ * CUDA graph on the first call and replayed by later calls whose batch fits
+ * the context's workspace (it grows, and the chain is captured again, for a
+ * larger batch; option "batch_graph").  The call synchronizes the context's
+ * stream. */
 phj_status phj_batch_run(phj_ctx *ctx, uint32_t n, const phj_table *const *builds, const phj_table *const *probes,
                          phj_output **outs, phj_batch_result *result);
 

@@ -55,7 +55,7 @@ void begin_run(phj_ctx * ctx)
 KTimer::KTimer(phj_ctx * c, const char * name, uint64_t rows, uint64_t bytes)
     : ctx(c)
 {
-    if (!ctx->time_kernels)
+    if (!ctx->time_kernels || !name)
         return;
     KernelRecord r;
     r.name = name;
@@ -1672,6 +1672,7 @@ void phj_ctx_destroy(phj_ctx * ctx)
         DeviceScope dev(ctx);
         if (ctx->stream)
             cudaStreamSynchronize(ctx->stream);
+        free_batch_graph(ctx);
         if (ctx->l2_flush)
             cudaFree(ctx->l2_flush);
         if (ctx->d_err)
@@ -1734,6 +1735,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->chj_windows = (uint32_t)value;
     else if (std::strcmp(name, "bep_engine") == 0 && (value == 0 || value == 1))
         ctx->bep_engine = (int)value;
+    else if (std::strcmp(name, "batch_graph") == 0 && (value == 0 || value == 1))
+        ctx->batch_graph = (int)value;
     else if (std::strcmp(name, "probe_pass_bits") == 0 && value >= 0 && value <= 11)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
@@ -1771,6 +1774,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->chj_windows;
     else if (std::strcmp(name, "bep_engine") == 0)
         *value = ctx->bep_engine;
+    else if (std::strcmp(name, "batch_graph") == 0)
+        *value = ctx->batch_graph;
     else if (std::strcmp(name, "probe_pass_bits") == 0)
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)

@@ -23,12 +23,20 @@
 //                    reservation of output rows per step in the join's
 //                    output.  A partition with more build rows than the
 //                    shared table holds is built and probed in pieces.
+// The chain (counter clears, the three kernels, the scans and cursor
+// copies) reads no size back to the host: the join count and the joins'
+// prefix arrays and descriptors are uploaded in one copy into a workspace
+// the context keeps, the kernels read the count from there, and the chain
+// is captured once into a CUDA graph at the workspace's capacity and
+// replayed for every later batch that fits (option "batch_graph"; 0
+// launches the same chain at the batch's own sizes, with each kernel timed).
 // Each join's output is sized for one row per probe row; a join with more
 // (repeated build keys) is counted exactly, flagged, and run again alone.
 // Output multisets equal those of the single-join entry points; the order
 // of the rows is not fixed.
 #include "internal.h"
 
+#include <cstring>
 #include <numeric>
 
 namespace phjg
@@ -95,10 +103,12 @@ __device__ __forceinline__ TileRef tile_ref(const BatchJoin * d, uint32_t n, con
     return x;
 }
 
-__global__ void __launch_bounds__(kTNT) k_bt_hist(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ tb,
-                                                  const uint64_t * __restrict__ tp, uint32_t * __restrict__ cnt_b, uint32_t * __restrict__ cnt_p)
+__global__ void __launch_bounds__(kTNT) k_bt_hist(const BatchJoin * __restrict__ d, const uint32_t * __restrict__ d_n,
+                                                  const uint64_t * __restrict__ tb, const uint64_t * __restrict__ tp,
+                                                  uint32_t * __restrict__ cnt_b, uint32_t * __restrict__ cnt_p)
 {
     __shared__ uint32_t h[1u << 11];
+    const uint32_t n = *d_n;
     const uint64_t n_tiles = tb[n] + tp[n];
     for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x)
     {
@@ -122,13 +132,14 @@ __global__ void __launch_bounds__(kTNT) k_bt_hist(const BatchJoin * __restrict__
 // Rows of the tile to their partitions: one reservation per partition and
 // tile on the running cursors (offsets over all joins' partitions), the
 // row's rank inside the tile's share from a shared counter.
-__global__ void __launch_bounds__(kTNT) k_bt_scatter(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ tb,
-                                                     const uint64_t * __restrict__ tp, const uint32_t * __restrict__ off_b,
-                                                     const uint32_t * __restrict__ off_p, uint32_t * __restrict__ cur_b,
-                                                     uint32_t * __restrict__ cur_p)
+__global__ void __launch_bounds__(kTNT) k_bt_scatter(const BatchJoin * __restrict__ d, const uint32_t * __restrict__ d_n,
+                                                     const uint64_t * __restrict__ tb, const uint64_t * __restrict__ tp,
+                                                     const uint32_t * __restrict__ off_b, const uint32_t * __restrict__ off_p,
+                                                     uint32_t * __restrict__ cur_b, uint32_t * __restrict__ cur_p)
 {
     __shared__ uint32_t h[1u << 11];
     __shared__ uint32_t base[1u << 11];
+    const uint32_t n = *d_n;
     const uint64_t n_tiles = tb[n] + tp[n];
     for (uint64_t t = blockIdx.x; t < n_tiles; t += gridDim.x)
     {
@@ -169,7 +180,8 @@ __global__ void __launch_bounds__(kTNT) k_bt_scatter(const BatchJoin * __restric
 // The persistent join: CTAs pop (join, partition) items until the queue is
 // empty.  out_cur[j] counts join j's output rows (also past its capacity,
 // where nothing is written and over[j] is set).
-__global__ void __launch_bounds__(kJNT) k_bt_join(const BatchJoin * __restrict__ d, uint32_t n, const uint64_t * __restrict__ parts,
+__global__ void __launch_bounds__(kJNT) k_bt_join(const BatchJoin * __restrict__ d, const uint32_t * __restrict__ d_n,
+                                                  const uint64_t * __restrict__ parts,
                                                   const uint32_t * __restrict__ off_b, const uint32_t * __restrict__ off_p,
                                                   unsigned int * __restrict__ next_item, unsigned long long * __restrict__ out_cur,
                                                   int * __restrict__ over)
@@ -179,6 +191,7 @@ __global__ void __launch_bounds__(kJNT) k_bt_join(const BatchJoin * __restrict__
     __shared__ uint32_t ws[kJNT / 32];
     __shared__ uint32_t s_item;
     __shared__ unsigned long long s_out;
+    const uint32_t n = *d_n;
     const uint64_t n_items = parts[n];
     for (;;)
     {
@@ -272,6 +285,175 @@ uint32_t partition_bits(uint64_t build_rows)
     return b;
 }
 
+size_t round_up(size_t x, size_t a)
+{
+    return (x + a - 1) / a * a;
+}
+} // namespace
+
+// The chain's workspace, kept by the context across batches at fixed
+// addresses, so that one captured graph of the chain replays for every
+// batch of at most n_cap joins and q_cap partitions in all.  Device block:
+// the upload region (join count, the three prefix arrays, the join
+// descriptors), then the per-join output counters and overflow flags
+// (adjacent: one download), then the partitions' counts, offsets and
+// cursors and the scan's carry space.  Pinned host block: the upload
+// staging at the same offsets, then the download staging.
+struct BatchGraph
+{
+    uint32_t n_cap = 0;
+    uint64_t q_cap = 0;
+    uint8_t * dev = nullptr;
+    uint8_t * host = nullptr;
+    size_t o_tb = 0, o_tp = 0, o_parts = 0, o_desc = 0, o_out = 0, o_cnt = 0, o_carry = 0, o_next = 0, bytes = 0;
+    cudaGraphExec_t exec = nullptr;
+    uint64_t kernels = 0; // kernel launches in one replay
+};
+
+void free_batch_graph(phj_ctx * ctx)
+{
+    BatchGraph * W = ctx->batch_ws;
+    if (!W)
+        return;
+    if (W->exec)
+        cudaGraphExecDestroy(W->exec);
+    if (W->dev)
+        cudaFree(W->dev);
+    if (W->host)
+        cudaFreeHost(W->host);
+    delete W;
+    ctx->batch_ws = nullptr;
+}
+
+namespace
+{
+struct Chain
+{
+    const uint8_t * base;
+    const BatchGraph * W;
+    uint32_t * n() const { return (uint32_t *)base; }
+    uint64_t * tb() const { return (uint64_t *)(base + W->o_tb); }
+    uint64_t * tp() const { return (uint64_t *)(base + W->o_tp); }
+    uint64_t * parts() const { return (uint64_t *)(base + W->o_parts); }
+    BatchJoin * desc() const { return (BatchJoin *)(base + W->o_desc); }
+    unsigned long long * out_cur() const { return (unsigned long long *)(base + W->o_out); }
+    int * over() const { return (int *)(base + W->o_out + 8ull * W->n_cap); }
+    uint32_t * cnt(int k) const { return (uint32_t *)(base + W->o_cnt) + (uint64_t)k * (W->q_cap + 1); } // cnt_b, cnt_p, off_b, off_p, cur_b, cur_p
+    uint32_t * carry() const { return (uint32_t *)(base + W->o_carry); }
+    unsigned int * next() const { return (unsigned int *)(base + W->o_next); }
+};
+
+BatchGraph & batch_workspace(phj_ctx * ctx, uint32_t n, uint64_t nq)
+{
+    BatchGraph * W = ctx->batch_ws;
+    if (W && n <= W->n_cap && nq <= W->q_cap)
+        return *W;
+    uint32_t n_cap = W ? W->n_cap : 16;
+    uint64_t q_cap = W ? W->q_cap : 4096;
+    while (n_cap < n)
+        n_cap *= 2;
+    while (q_cap < nq)
+        q_cap *= 2;
+    PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+    free_batch_graph(ctx);
+    W = new BatchGraph;
+    ctx->batch_ws = W;
+    W->n_cap = n_cap;
+    W->q_cap = q_cap;
+    size_t at = 0;
+    auto take = [&](size_t bytes) {
+        const size_t o = at;
+        at = round_up(at + bytes, 256);
+        return o;
+    };
+    take(sizeof(uint32_t));
+    W->o_tb = take(8ull * (n_cap + 1));
+    W->o_tp = take(8ull * (n_cap + 1));
+    W->o_parts = take(8ull * (n_cap + 1));
+    W->o_desc = take(sizeof(BatchJoin) * n_cap);
+    W->o_out = take(12ull * n_cap);
+    W->o_cnt = take(6 * 4ull * (q_cap + 1));
+    W->o_carry = take(4ull * std::max<uint64_t>(scan_u32_carry(q_cap), 1));
+    W->o_next = take(sizeof(unsigned int));
+    W->bytes = at;
+    PHJ_CUDA(cudaMalloc(&W->dev, W->bytes));
+    PHJ_CUDA(cudaMallocHost(&W->host, W->o_cnt));
+    return *W;
+}
+
+// The chain on the context's stream: counts, offsets and cursors of q_len
+// partitions (zero past the batch's own), then the three kernels.  With
+// `bytes` (rows, input bytes) each kernel is timed; without, nothing but
+// stream work is issued, so the chain can be captured.
+void enqueue_chain(phj_ctx * ctx, const Chain & c, uint64_t q_len, unsigned tgrid, unsigned jgrid, const uint64_t * bytes)
+{
+    cudaStream_t st = ctx->stream;
+    const uint64_t q_bytes = (q_len + 1) * sizeof(uint32_t);
+    uint32_t *cnt_b = c.cnt(0), *cnt_p = c.cnt(1), *off_b = c.cnt(2), *off_p = c.cnt(3), *cur_b = c.cnt(4), *cur_p = c.cnt(5);
+    PHJ_CUDA(cudaMemsetAsync(cnt_b, 0, q_bytes, st));
+    PHJ_CUDA(cudaMemsetAsync(cnt_p, 0, q_bytes, st));
+    PHJ_CUDA(cudaMemsetAsync(c.next(), 0, sizeof(unsigned int), st));
+    PHJ_CUDA(cudaMemsetAsync(c.out_cur(), 0, 12ull * c.W->n_cap, st));
+    {
+        KTimer kt(ctx, bytes ? "batch_hist" : nullptr, bytes ? bytes[0] : 0, bytes ? bytes[0] * 8 : 0);
+        k_bt_hist<<<tgrid, kTNT, 0, st>>>(c.desc(), c.n(), c.tb(), c.tp(), cnt_b, cnt_p);
+        PHJ_LAUNCHED(ctx, "batch_hist");
+    }
+    scan_u32_into(ctx, cnt_b, off_b, q_len, c.carry());
+    scan_u32_into(ctx, cnt_p, off_p, q_len, c.carry());
+    PHJ_CUDA(cudaMemcpyAsync(cur_b, off_b, q_bytes, cudaMemcpyDeviceToDevice, st));
+    PHJ_CUDA(cudaMemcpyAsync(cur_p, off_p, q_bytes, cudaMemcpyDeviceToDevice, st));
+    {
+        KTimer kt(ctx, bytes ? "batch_scatter" : nullptr, bytes ? bytes[0] : 0, bytes ? 2 * bytes[1] : 0);
+        k_bt_scatter<<<tgrid, kTNT, 0, st>>>(c.desc(), c.n(), c.tb(), c.tp(), off_b, off_p, cur_b, cur_p);
+        PHJ_LAUNCHED(ctx, "batch_scatter");
+    }
+    {
+        KTimer kt(ctx, bytes ? "batch_join" : nullptr, bytes ? bytes[2] : 0, bytes ? bytes[1] : 0);
+        k_bt_join<<<jgrid, kJNT, 0, st>>>(c.desc(), c.n(), c.parts(), off_b, off_p, c.next(), c.out_cur(), c.over());
+        PHJ_LAUNCHED(ctx, "batch_join");
+    }
+}
+
+unsigned join_grid(phj_ctx * ctx)
+{
+    int per_sm = 0;
+    PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bt_join, kJNT, 0));
+    return (unsigned)ctx->num_sms * (unsigned)std::max(per_sm, 1);
+}
+
+// Captures the chain at the workspace's capacity (every grid at its
+// largest: CTAs past the batch's tiles and partitions find no work) and
+// instantiates it.
+void capture_chain(phj_ctx * ctx, BatchGraph & W)
+{
+    const unsigned jgrid = join_grid(ctx);
+    const uint64_t before = ctx->launches;
+    cudaGraph_t g = nullptr;
+    PHJ_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    try
+    {
+        enqueue_chain(ctx, Chain{W.dev, &W}, W.q_cap, (unsigned)ctx->num_sms * 8, jgrid, nullptr);
+    }
+    catch (...)
+    {
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g)
+            cudaGraphDestroy(g);
+        cudaGetLastError();
+        ctx->launches = before;
+        throw;
+    }
+    PHJ_CUDA(cudaStreamEndCapture(ctx->stream, &g));
+    W.kernels = ctx->launches - before;
+    ctx->launches = before;
+    const cudaError_t e = cudaGraphInstantiate(&W.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess)
+        W.exec = nullptr;
+    PHJ_CUDA(e);
+}
+
 void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, const phj_table * const * probes, phj_output ** outs,
                phj_batch_result * res)
 {
@@ -289,7 +471,7 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
 
     std::vector<BatchJoin> h(n);
     std::vector<uint64_t> tb(n + 1, 0), tp(n + 1, 0), parts(n + 1, 0);
-    uint64_t brows = 0, prows = 0;
+    uint64_t brows = 0, prows = 0, in_bytes = 0;
     for (uint32_t j = 0; j < n; ++j)
     {
         const phj_table & B = *builds[j];
@@ -309,31 +491,11 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
         tp[j + 1] = tp[j] + ceil_div(P.rows, kTile);
         brows += B.rows;
         prows += P.rows;
+        in_bytes += B.rows * (8 + schema_bytes(B.schema)) + P.rows * (8 + schema_bytes(P.schema));
     }
     if (brows >= (1ull << 32) || prows >= (1ull << 32))
         throw Error(PHJ_ERR_UNSUPPORTED, "batch: fewer than 2^32 build rows and 2^32 probe rows in all");
     const uint64_t NQ = parts[n];
-    uint32_t * cnt_b = s.get<uint32_t>(NQ + 1);
-    uint32_t * cnt_p = s.get<uint32_t>(NQ + 1);
-    uint32_t * off_b = s.get<uint32_t>(NQ + 1);
-    uint32_t * off_p = s.get<uint32_t>(NQ + 1);
-    uint32_t * cur_b = s.get<uint32_t>(NQ + 1);
-    uint32_t * cur_p = s.get<uint32_t>(NQ + 1);
-    uint64_t * d_tb = s.get<uint64_t>(n + 1);
-    uint64_t * d_tp = s.get<uint64_t>(n + 1);
-    uint64_t * d_parts = s.get<uint64_t>(n + 1);
-    unsigned int * next_item = s.get<unsigned int>(1);
-    unsigned long long * out_cur = s.get<unsigned long long>(std::max<uint32_t>(n, 1));
-    int * over = s.get<int>(std::max<uint32_t>(n, 1));
-    BatchJoin * d_desc = s.get<BatchJoin>(std::max<uint32_t>(n, 1));
-    PHJ_CUDA(cudaMemsetAsync(cnt_b, 0, (NQ + 1) * sizeof(uint32_t), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(cnt_p, 0, (NQ + 1) * sizeof(uint32_t), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(next_item, 0, sizeof(unsigned int), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(out_cur, 0, std::max<uint32_t>(n, 1) * sizeof(unsigned long long), ctx->stream));
-    PHJ_CUDA(cudaMemsetAsync(over, 0, std::max<uint32_t>(n, 1) * sizeof(int), ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(d_tb, tb.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(d_tp, tp.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
-    PHJ_CUDA(cudaMemcpyAsync(d_parts, parts.data(), (n + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice, ctx->stream));
 
     // outputs at one row per probe row (exact for unique build keys)
     std::vector<phj_output *> made(n, nullptr);
@@ -350,45 +512,42 @@ void run_batch(phj_ctx * ctx, uint32_t n, const phj_table * const * builds, cons
                 J.out_r[c] = made[j]->rcol[c];
             J.out_cap = probes[j]->rows;
         }
-        PHJ_CUDA(cudaMemcpyAsync(d_desc, h.data(), n * sizeof(BatchJoin), cudaMemcpyHostToDevice, ctx->stream));
-        const uint64_t n_tiles = tb[n] + tp[n];
-        const unsigned tgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->num_sms * 8));
-        if (n_tiles)
-        {
-            {
-                KTimer kt(ctx, "batch_hist", brows + prows, (brows + prows) * 8);
-                k_bt_hist<<<tgrid, kTNT, 0, ctx->stream>>>(d_desc, n, d_tb, d_tp, cnt_b, cnt_p);
-                PHJ_LAUNCHED(ctx, "batch_hist");
-            }
-            scan_u32(ctx, s, cnt_b, off_b, NQ);
-            scan_u32(ctx, s, cnt_p, off_p, NQ);
-            PHJ_CUDA(cudaMemcpyAsync(cur_b, off_b, (NQ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
-            PHJ_CUDA(cudaMemcpyAsync(cur_p, off_p, (NQ + 1) * sizeof(uint32_t), cudaMemcpyDeviceToDevice, ctx->stream));
-            uint64_t in_bytes = 0;
-            for (uint32_t j = 0; j < n; ++j)
-                in_bytes += builds[j]->rows * (8 + schema_bytes(builds[j]->schema)) + probes[j]->rows * (8 + schema_bytes(probes[j]->schema));
-            {
-                KTimer kt(ctx, "batch_scatter", brows + prows, 2 * in_bytes);
-                k_bt_scatter<<<tgrid, kTNT, 0, ctx->stream>>>(d_desc, n, d_tb, d_tp, off_b, off_p, cur_b, cur_p);
-                PHJ_LAUNCHED(ctx, "batch_scatter");
-            }
-            int per_sm = 0;
-            PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_bt_join, kJNT, 0));
-            const unsigned jgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(NQ, (uint64_t)ctx->num_sms * std::max(per_sm, 1)));
-            {
-                KTimer kt(ctx, "batch_join", prows, in_bytes);
-                k_bt_join<<<jgrid, kJNT, 0, ctx->stream>>>(d_desc, n, d_parts, off_b, off_p, next_item, out_cur, over);
-                PHJ_LAUNCHED(ctx, "batch_join");
-            }
-        }
         std::vector<unsigned long long> rows(n, 0);
         std::vector<int> ov(n, 0);
         if (n)
         {
-            PHJ_CUDA(cudaMemcpyAsync(rows.data(), out_cur, n * sizeof(unsigned long long), cudaMemcpyDeviceToHost, ctx->stream));
-            PHJ_CUDA(cudaMemcpyAsync(ov.data(), over, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            BatchGraph & W = batch_workspace(ctx, n, NQ);
+            // one upload: join count, prefix arrays, descriptors
+            uint8_t * H = W.host;
+            std::memcpy(H, &n, sizeof(uint32_t));
+            std::memcpy(H + W.o_tb, tb.data(), (n + 1) * sizeof(uint64_t));
+            std::memcpy(H + W.o_tp, tp.data(), (n + 1) * sizeof(uint64_t));
+            std::memcpy(H + W.o_parts, parts.data(), (n + 1) * sizeof(uint64_t));
+            std::memcpy(H + W.o_desc, h.data(), n * sizeof(BatchJoin));
+            PHJ_CUDA(cudaMemcpyAsync(W.dev, H, W.o_desc + n * sizeof(BatchJoin), cudaMemcpyHostToDevice, ctx->stream));
+            const Chain c{W.dev, &W};
+            if (ctx->batch_graph)
+            {
+                if (!W.exec)
+                    capture_chain(ctx, W);
+                KTimer kt(ctx, "batch_graph", brows + prows, (brows + prows) * 8 + 3 * in_bytes);
+                PHJ_CUDA(cudaGraphLaunch(W.exec, ctx->stream));
+                ctx->launches += W.kernels;
+            }
+            else
+            {
+                const uint64_t n_tiles = tb[n] + tp[n];
+                const unsigned tgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(n_tiles, (uint64_t)ctx->num_sms * 8));
+                const unsigned jgrid = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(NQ, join_grid(ctx)));
+                const uint64_t bytes[3] = {brows + prows, in_bytes, prows};
+                enqueue_chain(ctx, c, NQ, tgrid, jgrid, bytes);
+            }
+            uint8_t * D = H + W.o_out;
+            PHJ_CUDA(cudaMemcpyAsync(D, c.out_cur(), 12ull * W.n_cap, cudaMemcpyDeviceToHost, ctx->stream));
+            PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
+            std::memcpy(rows.data(), D, n * sizeof(unsigned long long));
+            std::memcpy(ov.data(), D + 8ull * W.n_cap, n * sizeof(int));
         }
-        PHJ_CUDA(cudaStreamSynchronize(ctx->stream));
         uint64_t out_rows = 0;
         for (uint32_t j = 0; j < n; ++j)
         {

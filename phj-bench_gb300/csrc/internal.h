@@ -73,6 +73,12 @@ struct LeafMark
     uint32_t words = 0;
 };
 
+namespace phjg
+{
+struct BatchGraph; // batch.cu: phj_batch_run's workspace and captured chain
+void free_batch_graph(phj_ctx * ctx);
+} // namespace phjg
+
 struct phj_ctx
 {
     int device = 0;
@@ -109,6 +115,8 @@ struct phj_ctx
     int pack_build = 1;           // pack unique-key build payloads row-major for the projection (0: columns)
     uint32_t chj_windows = 0;     // CHJ: probe in this many windows of sub-tables (0 or 1: one sweep)
     int bep_engine = 0;           // PHJ/BEP: 0 the device budget engine, 1 budget-sized probe batches
+    int batch_graph = 1;          // phj_batch_run: 1 replays its chain as a CUDA graph, 0 launches it
+    phjg::BatchGraph * batch_ws = nullptr;
     uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)
     int64_t test_stuck_leaf = -1; // test hook: PHJ/BEP leaf left BUILDING before the probe
@@ -197,7 +205,8 @@ struct Scratch
 // ----- timing ----------------------------------------------------------------
 cudaEvent_t take_event(phj_ctx * ctx);
 void begin_run(phj_ctx * ctx);
-// Records an event pair around the next launch(es) when kernel timing is on.
+// Records an event pair around the next launch(es) when kernel timing is on
+// (and `name` is not null).
 struct KTimer
 {
     phj_ctx * ctx;
@@ -216,6 +225,10 @@ uint32_t max_width(const Cols & c);
 // ----- scan.cu -----------------------------------------------------------------
 // Exclusive scan of m u32 values into out[0..m); out[m] = total.
 void scan_u32(phj_ctx * ctx, Scratch & s, const uint32_t * in, uint32_t * out, uint64_t m);
+// The same with caller-owned carry space of scan_u32_carry(m) values (none
+// is allocated, so the launches can be captured into a CUDA graph).
+uint64_t scan_u32_carry(uint64_t m);
+void scan_u32_into(phj_ctx * ctx, const uint32_t * in, uint32_t * out, uint64_t m, uint32_t * carry);
 
 // ----- partition.cu ---------------------------------------------------------------
 // Radix-partitions n rows by the top sum(pass_bits) bits of intHash64(key)

@@ -64,7 +64,13 @@ __global__ void __launch_bounds__(kScanNT) k_scan_tile(const uint32_t * in, uint
 }
 } // namespace
 
-void scan_u32(phj_ctx * ctx, Scratch & s, const uint32_t * in, uint32_t * out, uint64_t m)
+uint64_t scan_u32_carry(uint64_t m)
+{
+    const uint64_t tiles = ceil_div(m, kScanTile);
+    return tiles <= 1 ? 0 : tiles + 1 + scan_u32_carry(tiles);
+}
+
+void scan_u32_into(phj_ctx * ctx, const uint32_t * in, uint32_t * out, uint64_t m, uint32_t * carry)
 {
     if (m == 0)
     {
@@ -78,12 +84,17 @@ void scan_u32(phj_ctx * ctx, Scratch & s, const uint32_t * in, uint32_t * out, u
         PHJ_LAUNCHED(ctx, "scan_tile");
         return;
     }
-    uint32_t * sums = s.get<uint32_t>(tiles + 1);
+    uint32_t * sums = carry;
     k_scan_reduce<<<(unsigned)tiles, kScanNT, 0, ctx->stream>>>(in, m, sums);
     PHJ_LAUNCHED(ctx, "scan_reduce");
-    scan_u32(ctx, s, sums, sums, tiles);
+    scan_u32_into(ctx, sums, sums, tiles, carry + tiles + 1);
     k_scan_tile<<<(unsigned)tiles, kScanNT, 0, ctx->stream>>>(in, m, sums, out);
     PHJ_LAUNCHED(ctx, "scan_tile");
 }
 
+void scan_u32(phj_ctx * ctx, Scratch & s, const uint32_t * in, uint32_t * out, uint64_t m)
+{
+    const uint64_t c = scan_u32_carry(m);
+    scan_u32_into(ctx, in, out, m, c ? s.get<uint32_t>(c) : nullptr);
+}
 } // namespace phjg

@@ -105,6 +105,44 @@ def test_batch_of_medium_joins_equals_the_oracle(ctx):
             t.free()
 
 
+def test_batch_graph_replays_equal_the_launched_chain(ctx):
+    """phj_batch_run replays its chain as a CUDA graph captured at the
+    workspace's capacity.  Batches of changing shape -- past the first
+    workspace's 16 joins and 4096 partitions (a new capture), then smaller
+    again (a replay with stale entries past the batch's own) -- give every
+    join the same rows as the chain launched at the batch's own sizes and
+    as the join alone."""
+    rng = np.random.default_rng(11)
+    shapes = [(3, 1_000, 30_000), (40, 50_000, 100_000), (5, 1, 20_000), (1, 0, 1), (2, 200_000, 400_000)]
+    for bi, (nj, lo, hi) in enumerate(shapes):
+        specs = [request(400 + 64 * bi + i, int(rng.integers(lo, hi)), 0, int(rng.integers(100, 1000)),
+                         [P.U64, P.U32][: 1 + i % 2], [P.U32, P.U16][: 1 + (i + 1) % 2]) for i in range(nj)]
+        specs = [(b, P.gen_spec(4, max(1, b.rows * int(rng.integers(2, 6))), p.seed, p.key_seed,
+                                [p.schema.types[k] for k in range(p.schema.n_payloads)], domain=max(b.rows, 1),
+                                match_permille=p.match_permille)) for b, p in specs]
+        tbs = [ctx.generate(b.kind, b.rows, b.seed, b.key_seed, [b.schema.types[k] for k in range(b.schema.n_payloads)])
+               for b, _ in specs]
+        tps = [ctx.generate(p.kind, p.rows, p.seed, p.key_seed, [p.schema.types[k] for k in range(p.schema.n_payloads)],
+                            domain=p.domain, match_permille=p.match_permille) for _, p in specs]
+        try:
+            fps = {}
+            for graph in (1, 0):
+                ctx.set_int("batch_graph", graph)
+                outs, res = ctx.run_batch(tbs, tps)
+                names = {k["name"] for k in ctx.kernel_times()}
+                assert ("batch_graph" in names) == bool(graph) and ("batch_join" in names) == (not graph)
+                fps[graph] = [tuple(o.fingerprint()) for o in outs]
+                for o in outs:
+                    o.free()
+            assert fps[1] == fps[0]
+            for (b, p), fp in zip(specs, fps[1]):
+                assert fp == tuple(alone_fingerprint(ctx, b, p))
+        finally:
+            ctx.set_int("batch_graph", 1)
+            for t in tbs + tps:
+                t.free()
+
+
 @pytest.mark.parametrize("mode", ["plain", "batched"])
 def test_served_results_equal_alone(ctx, mode):
     reqs = mix()
