@@ -649,7 +649,7 @@ def main():
                 e2e_t.append(t1 - t0)
         e2e_s = dist.max(statistics.mean(e2e_t))
         line["e2e"] = {"value": total_tuples / e2e_s, "unit": "tuples/s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-                       "ms_per_step": e2e_s * 1e3,
+                       "ms_per_step": e2e_s * 1e3, "runs_ms": [round(t * 1e3, 2) for t in e2e_t],
                        "path": {"phj-pure": "phj_run_phj_pure_host (pinned host inputs and output columns)",
                                 "phj": "phj_run_phj_bep_host (pinned host inputs and output columns)"}.get(
                                     scheme, "phj_table_upload + scheme + phj_output_download")}

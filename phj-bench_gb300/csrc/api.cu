@@ -1737,6 +1737,8 @@ phj_status phj_ctx_set_int(phj_ctx * ctx, const char * name, int64_t value)
         ctx->bep_engine = (int)value;
     else if (std::strcmp(name, "batch_graph") == 0 && (value == 0 || value == 1))
         ctx->batch_graph = (int)value;
+    else if (std::strcmp(name, "probe_fused") == 0 && (value == 0 || value == 1))
+        ctx->probe_fused = (int)value;
     else if (std::strcmp(name, "probe_pass_bits") == 0 && value >= 0 && value <= 11)
         ctx->probe_pass_bits = (uint32_t)value;
     else if (std::strcmp(name, "test_stuck_leaf") == 0 && value >= -1)
@@ -1776,6 +1778,8 @@ phj_status phj_ctx_get_int(const phj_ctx * ctx, const char * name, int64_t * val
         *value = ctx->bep_engine;
     else if (std::strcmp(name, "batch_graph") == 0)
         *value = ctx->batch_graph;
+    else if (std::strcmp(name, "probe_fused") == 0)
+        *value = ctx->probe_fused;
     else if (std::strcmp(name, "probe_pass_bits") == 0)
         *value = ctx->probe_pass_bits;
     else if (std::strcmp(name, "test_stuck_leaf") == 0)

@@ -281,6 +281,45 @@ __device__ __forceinline__ void bulk_copy_g2s(void * dst, const void * src, uint
                  : "memory");
 }
 
+// An L2 cache policy that evicts the lines it touches first: for data read
+// once (streamed probe rows), so it does not push out tables still in use.
+__device__ __forceinline__ uint64_t l2_evict_first()
+{
+    uint64_t p;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// 8-byte asynchronous copy from global to shared memory (cp.async: no
+// register waits for the value) under the L2 cache policy `pol`; dst and
+// src 8-byte aligned.  A thread's copies are complete after its
+// cp_async_wait_all.
+__device__ __forceinline__ void cp_async8(void * dst, const void * src, uint64_t pol)
+{
+    asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "l"(pol) : "memory");
+}
+
+// 16-byte asynchronous copy from global to shared memory through L2 only;
+// dst and src 16-byte aligned.
+__device__ __forceinline__ void cp_async16(void * dst, const void * src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all()
+{
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+// A shared-memory read the compiler may not fold into an earlier value held
+// in a register.
+__device__ __forceinline__ uint64_t ld_shared_u64(const uint64_t * p)
+{
+    uint64_t v;
+    asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+
 // Bulk prefetch of [src, src + bytes) into L2 by the TMA engine (no
 // registers, no shared memory); src 16-byte aligned, bytes % 16 == 0.
 __device__ __forceinline__ void bulk_prefetch_l2(const void * src, uint32_t bytes)

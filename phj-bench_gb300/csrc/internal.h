@@ -116,6 +116,7 @@ struct phj_ctx
     uint32_t chj_windows = 0;     // CHJ: probe in this many windows of sub-tables (0 or 1: one sweep)
     int bep_engine = 0;           // PHJ/BEP: 0 the device budget engine, 1 budget-sized probe batches
     int batch_graph = 1;          // phj_batch_run: 1 replays its chain as a CUDA graph, 0 launches it
+    int probe_fused = 1;          // unique build keys, packed payloads: 1 looks up and projects in one kernel
     phjg::BatchGraph * batch_ws = nullptr;
     uint32_t probe_pass_bits = 0; // PHJ-PURE probe side's written pass (0: the first logical pass's bits)
     bool p1_beside = false;       // first radix passes run beside other kernels (register-capped scatter)

@@ -143,10 +143,170 @@ __device__ __forceinline__ void columns_pass(const Cols & src, void * const * ds
         }
 }
 
-// Lookups: per probe row its head build row (kNoMatch when the key is
-// absent), per warp chunk its number of output rows.  kWin (CHJ only):
+// Lookup of one warp chunk (kWChunk probe rows from chunk * kWChunk): per
+// row, its head build row (kNoMatch when the key is absent) and match count
+// go to the sink (sink(i, brow, count) for row i of the chunk; sink.key(i,
+// key) as each key is read); rows whose key lies past the first cell pair
+// wait in the warp's queue (qkey, qrow) and are probed after the chunk.
+// Returns this lane's share of the chunk's output rows.  kWin (CHJ only):
 // rows outside the sub-table window [a.win_lo, a.win_hi) touch no table and
 // record no match.
+template <int kMode, bool kDup, bool kWin, class Sink>
+__device__ __forceinline__ uint32_t lookup_chunk(const ProbeArgs & a, uint64_t chunk, uint32_t lane, uint64_t * qkey, uint16_t * qrow,
+                                                 const Sink & sink)
+{
+    const uint32_t shift = 64u - a.leaf_bits;
+    const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
+    const uint64_t ucap = 1ull << ulog;
+    const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
+    uint64_t key[kPRPT];
+    uint32_t live = 0;
+#pragma unroll
+    for (int k = 0; k < kPRPT; ++k)
+    {
+        const uint64_t row = row0 + (uint64_t)k * 32;
+        key[k] = 0;
+        if (row < a.probe_rows)
+        {
+            key[k] = __ldcs(a.probe.keys + row);
+            live |= 1u << k;
+            sink.key(k * 32 + lane, key[k]);
+        }
+    }
+    uint32_t total = 0;
+    uint32_t qn = 0; // rows in the warp's queue
+    // four directory loads (per-leaf tables), four first-cell loads,
+    // then the comparisons: four table requests in flight per lane
+#pragma unroll
+    for (int g = 0; g < kPRPT; g += 4)
+    {
+        ulonglong2 mv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            mv[u] = make_ulonglong2(0ull, 0ull);
+            if (kWin && (live >> (g + u) & 1u) && (uint32_t)(int_hash64(key[g + u]) >> shift) - a.win_lo >= a.win_hi - a.win_lo)
+                continue; // outside the window: the directory entry stays empty (no table)
+            if (kMode != kLeafUniform && (live >> (g + u) & 1u))
+                mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
+        }
+        CellPair cell[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const int k = g + u;
+            cell[u].a = make_ulonglong2(0ull, INVALID_REF);
+            cell[u].b = cell[u].a;
+            if (!(live >> k & 1u))
+                continue;
+            const uint64_t h = int_hash64(key[k]);
+            if (kMode == kLeafUniform)
+                cell[u] = load_pair<false>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
+            else if ((mv[u].y >> 40) & 0xffu)
+                cell[u] = load_pair<false>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const int k = g + u;
+            uint32_t brow = kNoMatch, mcnt = 0;
+            // the pair's two cells are the first two probe positions
+            uint64_t head = INVALID_REF;
+            bool more = false;
+            if (ref_valid(cell[u].a.y))
+            {
+                if (cell[u].a.x == key[k])
+                    head = cell[u].a.y;
+                else if (ref_valid(cell[u].b.y))
+                {
+                    if (cell[u].b.x == key[k])
+                        head = cell[u].b.y;
+                    else
+                        more = true;
+                }
+            }
+            {
+                // rows whose key lies past the cell pair wait in the
+                // warp's queue and are probed together after the chunk
+                const uint32_t m = __ballot_sync(0xffffffffu, more);
+                if (more)
+                {
+                    const uint32_t slot = qn + __popc(m & ((1u << lane) - 1u));
+                    qkey[slot] = key[k];
+                    qrow[slot] = (uint16_t)(k * 32 + lane);
+                }
+                qn += __popc(m);
+            }
+            if (!more)
+            {
+                if (ref_valid(head))
+                {
+                    brow = build_row_of<kMode>(head, a);
+                    const bool leaf_dup = kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
+                    if (kDup && kMode != kChj && a.grouped)
+                        mcnt = ref_block(head) ? ref_block(head) : 1u; // grouped: {count, first row}
+                    else
+                        mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
+                    total += mcnt;
+                }
+            }
+            if ((live >> k & 1u) && !more)
+                sink(k * 32 + lane, brow, mcnt);
+        }
+    }
+    {
+        __syncwarp();
+        for (uint32_t j = lane; j < qn; j += 32)
+        {
+            const uint64_t qk = qkey[j];
+            const uint64_t h = int_hash64(qk);
+            uint64_t head;
+            bool leaf_dup = true;
+            if (kMode == kLeafUniform)
+                head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, qk);
+            else
+            {
+                const ulonglong2 m = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(h >> shift)));
+                const uint64_t c = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
+                head = table_find_from(a.cells + m.x, c, probe_start(h, c) + 2, qk);
+                leaf_dup = ((m.y >> 48) & 1u) != 0;
+            }
+            uint32_t brow = kNoMatch, mcnt = 0;
+            if (ref_valid(head))
+            {
+                brow = build_row_of<kMode>(head, a);
+                if (kDup && kMode != kChj && a.grouped)
+                    mcnt = ref_block(head) ? ref_block(head) : 1u;
+                else
+                    mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
+                total += mcnt;
+            }
+            sink(qrow[j], brow, mcnt);
+        }
+        __syncwarp();
+    }
+    return total;
+}
+
+// Lookup results to global memory: the head array and (keys repeat) the
+// per-row match counts.
+template <bool kDup>
+struct HeadSink
+{
+    uint32_t * heads;
+    uint32_t * row_cnt;
+    uint64_t row0; // first row of the chunk
+    __device__ __forceinline__ void key(uint32_t, uint64_t) const {}
+    __device__ __forceinline__ void operator()(uint32_t i, uint32_t brow, uint32_t mcnt) const
+    {
+        heads[row0 + i] = brow;
+        if (kDup && row_cnt)
+            row_cnt[row0 + i] = mcnt;
+    }
+};
+
+// Lookups: per probe row its head build row (kNoMatch when the key is
+// absent), per warp chunk its number of output rows.
 template <int kMode, bool kDup, bool kWin = false>
 __global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant__ ProbeArgs a, uint32_t * __restrict__ heads,
                                                        uint32_t * __restrict__ counts)
@@ -154,9 +314,6 @@ __global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant_
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
     const uint64_t n_workers = ((uint64_t)gridDim.x * kPNT) >> 5;
-    const uint32_t shift = 64u - a.leaf_bits;
-    const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
-    const uint64_t ucap = 1ull << ulog;
     __shared__ uint64_t q_key[kPWarps * kWChunk];
     __shared__ uint16_t q_row[kPWarps * kWChunk];
     uint64_t * qkey = q_key + (threadIdx.x >> 5) * kWChunk;
@@ -164,139 +321,8 @@ __global__ void __launch_bounds__(kPNT, 4) k_probe_lookup(const __grid_constant_
     unsigned long long grand = 0;
     for (uint64_t chunk = ((uint64_t)blockIdx.x * kPNT + threadIdx.x) >> 5; chunk < n_chunks; chunk += n_workers)
     {
-        const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
-        uint64_t key[kPRPT];
-        uint32_t live = 0;
-#pragma unroll
-        for (int k = 0; k < kPRPT; ++k)
-        {
-            const uint64_t row = row0 + (uint64_t)k * 32;
-            key[k] = 0;
-            if (row < a.probe_rows)
-            {
-                key[k] = __ldcs(a.probe.keys + row);
-                live |= 1u << k;
-            }
-        }
-        uint32_t total = 0;
-        uint32_t qn = 0; // rows in the warp's queue
-        // four directory loads (per-leaf tables), four first-cell loads,
-        // then the comparisons: four table requests in flight per lane
-#pragma unroll
-        for (int g = 0; g < kPRPT; g += 4)
-        {
-            ulonglong2 mv[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-            {
-                mv[u] = make_ulonglong2(0ull, 0ull);
-                if (kWin && (live >> (g + u) & 1u) && (uint32_t)(int_hash64(key[g + u]) >> shift) - a.win_lo >= a.win_hi - a.win_lo)
-                    continue; // outside the window: the directory entry stays empty (no table)
-                if (kMode != kLeafUniform && (live >> (g + u) & 1u))
-                    mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[g + u]) >> shift)));
-            }
-            CellPair cell[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-            {
-                const int k = g + u;
-                cell[u].a = make_ulonglong2(0ull, INVALID_REF);
-                cell[u].b = cell[u].a;
-                if (!(live >> k & 1u))
-                    continue;
-                const uint64_t h = int_hash64(key[k]);
-                if (kMode == kLeafUniform)
-                    cell[u] = load_pair<false>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
-                else if ((mv[u].y >> 40) & 0xffu)
-                    cell[u] = load_pair<false>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-            {
-                const int k = g + u;
-                uint32_t brow = kNoMatch, mcnt = 0;
-                // the pair's two cells are the first two probe positions
-                uint64_t head = INVALID_REF;
-                bool more = false;
-                if (ref_valid(cell[u].a.y))
-                {
-                    if (cell[u].a.x == key[k])
-                        head = cell[u].a.y;
-                    else if (ref_valid(cell[u].b.y))
-                    {
-                        if (cell[u].b.x == key[k])
-                            head = cell[u].b.y;
-                        else
-                            more = true;
-                    }
-                }
-                {
-                    // rows whose key lies past the cell pair wait in the
-                    // warp's queue and are probed together after the chunk
-                    const uint32_t m = __ballot_sync(0xffffffffu, more);
-                    if (more)
-                    {
-                        const uint32_t slot = qn + __popc(m & ((1u << lane) - 1u));
-                        qkey[slot] = key[k];
-                        qrow[slot] = (uint16_t)(k * 32 + lane);
-                    }
-                    qn += __popc(m);
-                }
-                if (!more)
-                {
-                    if (ref_valid(head))
-                    {
-                        brow = build_row_of<kMode>(head, a);
-                        const bool leaf_dup = kMode == kLeafUniform ? true : ((mv[u].y >> 48) & 1u) != 0;
-                        if (kDup && kMode != kChj && a.grouped)
-                            mcnt = ref_block(head) ? ref_block(head) : 1u; // grouped: {count, first row}
-                        else
-                            mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
-                        total += mcnt;
-                    }
-                }
-                if ((live >> k & 1u) && !more)
-                {
-                    heads[row0 + (uint64_t)k * 32] = brow;
-                    if (kDup && a.row_cnt)
-                        a.row_cnt[row0 + (uint64_t)k * 32] = mcnt;
-                }
-            }
-        }
-        {
-            __syncwarp();
-            for (uint32_t j = lane; j < qn; j += 32)
-            {
-                const uint64_t qk = qkey[j];
-                const uint64_t row = chunk * kWChunk + qrow[j];
-                const uint64_t h = int_hash64(qk);
-                uint64_t head;
-                bool leaf_dup = true;
-                if (kMode == kLeafUniform)
-                    head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, qk);
-                else
-                {
-                    const ulonglong2 m = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(h >> shift)));
-                    const uint64_t c = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
-                    head = table_find_from(a.cells + m.x, c, probe_start(h, c) + 2, qk);
-                    leaf_dup = ((m.y >> 48) & 1u) != 0;
-                }
-                uint32_t brow = kNoMatch, mcnt = 0;
-                if (ref_valid(head))
-                {
-                    brow = build_row_of<kMode>(head, a);
-                    if (kDup && kMode != kChj && a.grouped)
-                        mcnt = ref_block(head) ? ref_block(head) : 1u;
-                    else
-                        mcnt = (kDup && leaf_dup) ? chain_length(brow, a, kMode == kChj) : 1u;
-                    total += mcnt;
-                }
-                heads[row] = brow;
-                if (kDup && a.row_cnt)
-                    a.row_cnt[row] = mcnt;
-            }
-            __syncwarp();
-        }
+        const HeadSink<kDup> sink{heads, a.row_cnt, chunk * kWChunk};
+        uint32_t total = lookup_chunk<kMode, kDup, kWin>(a, chunk, lane, qkey, qrow, sink);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
             total += __shfl_xor_sync(0xffffffffu, total, o);
@@ -319,19 +345,19 @@ constexpr int kProjMinBlocks = 4;
 
 // One column over a lane's single-match rows of a half: four loads, then
 // four stores.  Output row of round k is base + rel[k].
-template <class T>
-__device__ __forceinline__ void project_column(const void * src_v, void * dst_v, const uint32_t (&sidx)[kPH], uint64_t base,
-                                               const uint32_t (&rel)[kPH], uint32_t one, bool gather)
+template <class T, int kN = kPH>
+__device__ __forceinline__ void project_column(const void * src_v, void * dst_v, const uint32_t (&sidx)[kN], uint64_t base,
+                                               const uint32_t (&rel)[kN], uint32_t one, bool gather)
 {
     const T * src = static_cast<const T *>(src_v);
     T * dst = static_cast<T *>(dst_v) + base;
-    T v[kPH];
+    T v[kN];
 #pragma unroll
-    for (int u = 0; u < kPH; ++u)
+    for (int u = 0; u < kN; ++u)
         if (one >> u & 1u)
             v[u] = gather ? __ldg(src + sidx[u]) : __ldcs(src + sidx[u]);
 #pragma unroll
-    for (int u = 0; u < kPH; ++u)
+    for (int u = 0; u < kN; ++u)
         if (one >> u & 1u)
             __stcs(dst + rel[u], v[u]);
 }
@@ -339,27 +365,27 @@ __device__ __forceinline__ void project_column(const void * src_v, void * dst_v,
 // All output columns, one switch instance for the loop.  Without 16-byte
 // columns (kWide false) the widest staged value is 8 bytes, which keeps the
 // plain projection at four CTAs per SM.
-template <bool kWide = true>
-__device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t (&brow)[kPH], const uint32_t (&prow)[kPH], uint64_t base,
-                                            const uint32_t (&rel)[kPH], uint32_t one)
+template <bool kWide = true, int kN = kPH>
+__device__ __forceinline__ void project_all(const ProjCols & pc, const uint32_t (&brow)[kN], const uint32_t (&prow)[kN], uint64_t base,
+                                            const uint32_t (&rel)[kN], uint32_t one)
 {
 #pragma unroll 1
     for (uint32_t c = 0; c < pc.n; ++c)
     {
         const bool g = pc.by_build[c] != 0;
-        uint32_t idx[kPH];
+        uint32_t idx[kN];
 #pragma unroll
-        for (int u = 0; u < kPH; ++u)
+        for (int u = 0; u < kN; ++u)
             idx[u] = g ? brow[u] : prow[u];
         switch (pc.width[c])
         {
-            case 1: project_column<uint8_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
-            case 2: project_column<uint16_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
-            case 4: project_column<uint32_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
-            case 8: project_column<uint64_t>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 1: project_column<uint8_t, kN>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 2: project_column<uint16_t, kN>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 4: project_column<uint32_t, kN>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
+            case 8: project_column<uint64_t, kN>(pc.src[c], pc.dst[c], idx, base, rel, one, g); break;
             default:
                 if constexpr (kWide)
-                    project_column<uint4>(pc.src[c], pc.dst[c], idx, base, rel, one, g);
+                    project_column<uint4, kN>(pc.src[c], pc.dst[c], idx, base, rel, one, g);
                 break;
         }
     }
@@ -434,13 +460,13 @@ struct PackedCols
 
 // One build payload column of a half from the gathered packed rows.  The
 // offset is a multiple of the width, so a value lies in one 8-byte half.
-template <class T>
-__device__ __forceinline__ void packed_column(const uint4 (&row)[kPH], uint32_t off, void * dst_v, uint64_t base, const uint32_t (&rel)[kPH],
+template <class T, int kN = kPH>
+__device__ __forceinline__ void packed_column(const uint4 (&row)[kN], uint32_t off, void * dst_v, uint64_t base, const uint32_t (&rel)[kN],
                                               uint32_t one)
 {
     T * dst = static_cast<T *>(dst_v) + base;
 #pragma unroll
-    for (int u = 0; u < kPH; ++u)
+    for (int u = 0; u < kN; ++u)
         if (one >> u & 1u)
         {
             if constexpr (sizeof(T) == 8)
@@ -513,6 +539,233 @@ __global__ void __launch_bounds__(kPNT, kWide ? 1 : 4) k_probe_project_packed(co
             }
             base += running;
         }
+    }
+}
+
+// The fused kernel's lookup of one warp chunk (no repeated build key): the
+// chunk's keys arrive in the warp's part of shared memory by asynchronous
+// copies (no register waits on them) and are read back four at a time for
+// the table loads; each row's head build row (kNoMatch when absent) goes to
+// brow_s; rows whose key lies past the first cell pair wait in the warp's
+// queue (their chunk rows in qrow) and are probed after the chunk.  Returns
+// this lane's number of matches.
+template <int kMode>
+__device__ __forceinline__ uint32_t fused_lookup(const ProbeArgs & a, uint64_t chunk, uint32_t lane, uint64_t * key_s, uint32_t * brow_s,
+                                                 uint16_t * qrow)
+{
+    const uint32_t shift = 64u - a.leaf_bits;
+    const uint32_t ulog = kMode == kLeafUniform ? (uint32_t)a.uniform_log2cap : 0u;
+    const uint64_t ucap = 1ull << ulog;
+    const uint64_t row0 = chunk * kWChunk + lane; // + k * 32
+    uint32_t live = 0;
+    const uint64_t stream = l2_evict_first(); // keys are read once
+#pragma unroll
+    for (int k = 0; k < kPRPT; ++k)
+    {
+        const uint64_t row = row0 + (uint64_t)k * 32;
+        if (row < a.probe_rows)
+        {
+            cp_async8(key_s + k * 32 + lane, a.probe.keys + row, stream);
+            live |= 1u << k;
+        }
+    }
+    cp_async_wait_all();
+    uint32_t total = 0;
+    uint32_t qn = 0;
+#pragma unroll
+    for (int g = 0; g < kPRPT; g += 4)
+    {
+        uint64_t key[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+            key[u] = (live >> (g + u) & 1u) ? ld_shared_u64(key_s + (g + u) * 32 + lane) : 0ull;
+        ulonglong2 mv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            mv[u] = make_ulonglong2(0ull, 0ull);
+            if (kMode != kLeafUniform && (live >> (g + u) & 1u))
+                mv[u] = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(int_hash64(key[u]) >> shift)));
+        }
+        CellPair cell[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            cell[u].a = make_ulonglong2(0ull, INVALID_REF);
+            cell[u].b = cell[u].a;
+            if (!(live >> (g + u) & 1u))
+                continue;
+            const uint64_t h = int_hash64(key[u]);
+            if (kMode == kLeafUniform)
+                cell[u] = load_pair<false>(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog) + probe_start(h, ucap));
+            else if ((mv[u].y >> 40) & 0xffu)
+                cell[u] = load_pair<false>(a.cells + mv[u].x + probe_start(h, 1ull << ((uint32_t)(mv[u].y >> 32) & 0xffu)));
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+        {
+            const uint32_t i = (uint32_t)(g + u) * 32 + lane;
+            uint64_t head = INVALID_REF;
+            bool more = false;
+            if (ref_valid(cell[u].a.y))
+            {
+                if (cell[u].a.x == key[u])
+                    head = cell[u].a.y;
+                else if (ref_valid(cell[u].b.y))
+                {
+                    if (cell[u].b.x == key[u])
+                        head = cell[u].b.y;
+                    else
+                        more = true;
+                }
+            }
+            const uint32_t m = __ballot_sync(0xffffffffu, more);
+            if (more)
+                qrow[qn + __popc(m & ((1u << lane) - 1u))] = (uint16_t)i;
+            qn += __popc(m);
+            if ((live >> (g + u) & 1u) && !more)
+            {
+                const uint32_t brow = ref_valid(head) ? build_row_of<kMode>(head, a) : kNoMatch;
+                total += brow != kNoMatch;
+                brow_s[i] = brow;
+            }
+        }
+    }
+    __syncwarp();
+    for (uint32_t j = lane; j < qn; j += 32)
+    {
+        const uint32_t i = qrow[j];
+        const uint64_t qk = key_s[i];
+        const uint64_t h = int_hash64(qk);
+        uint64_t head;
+        if (kMode == kLeafUniform)
+            head = table_find_from(a.cells + ((uint64_t)(uint32_t)(h >> shift) << ulog), ucap, probe_start(h, ucap) + 2, qk);
+        else
+        {
+            const ulonglong2 m = __ldg(reinterpret_cast<const ulonglong2 *>(a.meta + (uint32_t)(h >> shift)));
+            const uint64_t c = 1ull << ((uint32_t)(m.y >> 32) & 0xffu);
+            head = table_find_from(a.cells + m.x, c, probe_start(h, c) + 2, qk);
+        }
+        const uint32_t brow = ref_valid(head) ? build_row_of<kMode>(head, a) : kNoMatch;
+        total += brow != kNoMatch;
+        brow_s[i] = brow;
+    }
+    __syncwarp();
+    return total;
+}
+
+// Shared memory of one warp of the fused kernel: the build rows' gather
+// stage (half a chunk of 16-byte rows), the chunk's keys, head build rows
+// and queue; 44 KB a CTA, static, so three CTAs a SM leave L1 about 120 KB
+// (a 60 KB layout that also staged a probe payload column left about 70 KB
+// and ran 4.7 ms against 3.9 on 16M x 256M).
+constexpr uint32_t kFStage = 0, kFKeys = 2048, kFBrow = 4096, kFQueue = 5120, kFWarpBytes = 5632;
+
+// Lookup and projection in one pass, when no build key repeats and the
+// build payloads are packed.  A probe row then has at most one output row,
+// so the output is sized by the probe rows before the probe, and a warp
+// needs no offsets from other chunks: it looks its chunk up, reserves the
+// chunk's output rows with one atomic on the join's row counter, and
+// writes them -- no head array written and read back, no second read of
+// the probe keys.  Per half chunk, the build rows' 16-byte gathers go to
+// the warp's stage by asynchronous copies while the key column (from
+// shared memory) and the probe payload columns are written, then the build
+// payloads are written from the stage.  Warps take chunks by ticket (one
+// atomic a chunk).  A chunk's output rows are contiguous; chunks land in
+// reservation order.  pc holds the probe payload columns only.
+template <int kMode>
+__global__ void __launch_bounds__(kPNT, 3) k_probe_fused(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
+                                                      const __grid_constant__ PackedCols bc, uint64_t * __restrict__ out_keys,
+                                                      unsigned long long * __restrict__ out_rows, unsigned long long * __restrict__ tickets,
+                                                      uint64_t out_cap)
+{
+    __shared__ __align__(16) uint8_t fsm[kPWarps * kFWarpBytes];
+    const uint32_t lane = threadIdx.x & 31;
+    uint8_t * wsm = fsm + (threadIdx.x >> 5) * kFWarpBytes;
+    uint4 * stage = reinterpret_cast<uint4 *>(wsm + kFStage);
+    uint64_t * key_s = reinterpret_cast<uint64_t *>(wsm + kFKeys);
+    uint32_t * brow_s = reinterpret_cast<uint32_t *>(wsm + kFBrow);
+    uint16_t * qrow = reinterpret_cast<uint16_t *>(wsm + kFQueue);
+    const uint32_t n_chunks = (uint32_t)ceil_div(a.probe_rows, kWChunk); // probe rows < 2^32
+    // chunks in ticket order: the warps in flight stay within a few hundred
+    // chunks of each other, so the leaf tables and packed build rows of the
+    // buckets being probed stay in L2 (with a fixed stride per warp, warps
+    // drifted across buckets and the kernel read twice its bytes from DRAM)
+    unsigned long long t0 = 0;
+    if (lane == 0)
+        t0 = atomicAdd(tickets, 1ull);
+    uint32_t chunk = (uint32_t)__shfl_sync(0xffffffffu, t0, 0);
+    while (chunk < n_chunks)
+    {
+        unsigned long long tn = 0; // the next chunk's ticket, taken early
+        if (lane == 0)
+            tn = atomicAdd(tickets, 1ull);
+        uint32_t total = fused_lookup<kMode>(a, chunk, lane, key_s, brow_s, qrow);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            total += __shfl_xor_sync(0xffffffffu, total, o);
+        if (total == 0)
+        {
+            chunk = (uint32_t)__shfl_sync(0xffffffffu, tn, 0);
+            continue;
+        }
+        unsigned long long b0 = 0;
+        if (lane == 0)
+            b0 = atomicAdd(out_rows, (unsigned long long)total);
+        uint64_t base = __shfl_sync(0xffffffffu, b0, 0);
+#pragma unroll 1
+        for (int half = 0; half < 2; ++half)
+        {
+            const uint32_t i0 = (uint32_t)half * (kWChunk / 2) + lane;
+            uint32_t brow[kPH], prow[kPH], one = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                const uint32_t i = i0 + (uint32_t)k * 32;
+                const uint64_t row = (uint64_t)chunk * kWChunk + i;
+                prow[k] = (uint32_t)row;
+                brow[k] = row < a.probe_rows ? brow_s[i] : kNoMatch;
+                if (brow[k] != kNoMatch)
+                {
+                    one |= 1u << k;
+                    cp_async16(stage + k * 32 + lane, a.packed + brow[k]);
+                }
+            }
+            uint32_t rel[kPH], running = 0;
+#pragma unroll
+            for (int k = 0; k < kPH; ++k)
+            {
+                const uint32_t m = __ballot_sync(0xffffffffu, one >> k & 1u);
+                rel[k] = running + __popc(m & ((1u << lane) - 1u));
+                running += __popc(m);
+                if (base + rel[k] >= out_cap)
+                    one &= ~(1u << k);
+            }
+#pragma unroll
+            for (int u = 0; u < kPH; ++u)
+                if (one >> u & 1u)
+                    __stcs(out_keys + base + rel[u], key_s[i0 + (uint32_t)u * 32]);
+            project_all<false>(pc, brow, prow, base, rel, one);
+            cp_async_wait_all();
+            {
+                uint4 row[kPH];
+#pragma unroll
+                for (int u = 0; u < kPH; ++u)
+                    row[u] = stage[u * 32 + lane];
+#pragma unroll 1
+                for (uint32_t c = 0; c < bc.n; ++c)
+                    switch (bc.width[c])
+                    {
+                        case 1: packed_column<uint8_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        case 2: packed_column<uint16_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        case 4: packed_column<uint32_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                        default: packed_column<uint64_t>(row, bc.off[c], bc.dst[c], base, rel, one); break;
+                    }
+            }
+            base += running;
+            __syncwarp(); // the stage is refilled by the next half
+        }
+        chunk = (uint32_t)__shfl_sync(0xffffffffu, tn, 0);
     }
 }
 
@@ -898,8 +1151,91 @@ void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_
     dfree(ctx, b.flat);
 }
 
+// The fused probe: unique build keys with packed payloads, no 16-byte probe
+// payload column (its staged values would not fit the kernel's registers).
+static bool probe_fused_eligible(const phj_ctx * ctx, const ProbeArgs & a)
+{
+    bool narrow = true;
+    for (uint32_t c = 0; c < a.probe.n; ++c)
+        narrow = narrow && a.probe.width[c] <= 8;
+    return ctx->probe_fused && narrow && !a.any_dup && a.packed && a.win_hi == 0 && a.probe_rows > 0 && a.probe_rows < (1ull << 32);
+}
+
+// Unique build keys, packed build payloads: one pass that looks up and
+// projects (k_probe_fused) into an output of one row per probe row.
+static phj_output * probe_fused(phj_ctx * ctx, Scratch & s, const ProbeArgs & a, const phj_schema & left, const phj_schema & right)
+{
+    unsigned long long * counter = s.get<unsigned long long>(2); // output rows, chunk tickets
+    PHJ_CUDA(cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), ctx->stream));
+    phj_output * out = new_output(ctx, left, right, a.probe_rows);
+    try
+    {
+        OutCols o{};
+        o.keys = out->keys;
+        for (uint32_t c = 0; c < out->left.n_payloads; ++c)
+            o.left[c] = out->lcol[c];
+        for (uint32_t c = 0; c < out->right.n_payloads; ++c)
+            o.right[c] = out->rcol[c];
+        ProjCols pc{};
+        for (uint32_t c = 0; c < a.probe.n; ++c)
+        {
+            pc.src[pc.n] = a.probe.col[c];
+            pc.dst[pc.n] = o.right[c];
+            pc.width[pc.n] = a.probe.width[c];
+            pc.by_build[pc.n++] = 0;
+        }
+        PackedCols bc{};
+        for (uint32_t c = 0; c < a.build.n; ++c)
+        {
+            bc.dst[c] = o.left[c];
+            bc.width[c] = (uint8_t)a.build.width[c];
+            bc.off[c] = a.packed_off[c];
+        }
+        bc.n = a.build.n;
+        auto launch = [&](auto kernel) {
+            int per_sm = 0;
+            PHJ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPNT, 0));
+            const uint64_t n_chunks = ceil_div(a.probe_rows, kWChunk);
+            const unsigned grid = (unsigned)std::max<uint64_t>(
+                1, std::min<uint64_t>(ceil_div(n_chunks, kPWarps), (uint64_t)ctx->num_sms * (uint64_t)std::max(per_sm, 1)));
+            if (std::getenv("PHJ_DEBUG"))
+                std::fprintf(stderr, "[phj] probe_fused: grid %u x %d threads, %d CTAs/SM, chunks %llu\n", grid, kPNT, per_sm,
+                             (unsigned long long)n_chunks);
+            kernel<<<grid, kPNT, 0, ctx->stream>>>(a, pc, bc, o.keys, counter, counter + 1, a.probe_rows);
+        };
+        if ((a.uniform_log2cap >= 0 && a.uniform_log2cap < 1) || (reinterpret_cast<uintptr_t>(a.cells) & 31) != 0)
+            throw Error(PHJ_ERR_CUDA, "internal: leaf tables need aligned pairs of cells");
+        int rec = -1;
+        {
+            KTimer kt(ctx, "probe_fused", a.probe_rows, 0);
+            rec = kt.idx;
+            if (a.chj)
+                launch(k_probe_fused<kChj>);
+            else if (a.uniform_log2cap >= 0)
+                launch(k_probe_fused<kLeafUniform>);
+            else
+                launch(k_probe_fused<kLeafMeta>);
+            PHJ_LAUNCHED(ctx, "probe_fused");
+        }
+        unsigned long long total = 0;
+        read_small(ctx, {{&total, counter, sizeof(total)}});
+        out->rows = total;
+        // algorithmic bytes: every probe row read, every output row written
+        if (rec >= 0)
+            ctx->records[rec].bytes = a.probe_rows * row_bytes_of(a.probe, true) + total * (8 + row_bytes_of(a.build, false) + row_bytes_of(a.probe, false));
+    }
+    catch (...)
+    {
+        free_output(ctx, out);
+        throw;
+    }
+    return out;
+}
+
 phj_output * probe_join(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, const phj_schema & left, const phj_schema & right)
 {
+    if (probe_fused_eligible(ctx, a_in))
+        return probe_fused(ctx, s, a_in, left, right);
     ProbeArgs a = a_in;
     if ((a.grouped || a.any_dup) && !a.row_cnt)
         a.row_cnt = s.get<uint32_t>(std::max<uint64_t>(a.probe_rows, 1));

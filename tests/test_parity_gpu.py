@@ -406,6 +406,32 @@ def test_packed_build_payloads(ctx, pack, build_types):
         ctx.set_int("pack_build", 1)
 
 
+@pytest.mark.parametrize("probe_types", [[P.U32], [P.U64, P.U16], [], [P.U128, P.U8]])
+def test_fused_probe_equals_split_and_oracle(ctx, probe_types):
+    # Unique build keys with packed payloads: the probe looks up and
+    # projects in one kernel (probe_fused 1, output rows in reservation
+    # order) or in two (0); both give the oracle's rows.  A 16-byte probe
+    # column keeps the two-kernel form.
+    bt = [P.U64, P.U32]
+    bk = G.gen_keys(0, 9000, 41, 11)
+    b = P.BlockStream(bt, bk, G.payload_columns(42, bt, 9000))
+    rows = 256 * 37 + 5
+    p = P.BlockStream(probe_types, G.gen_keys(4, rows, 43, 11, domain=9000, match_permille=700),
+                      G.payload_columns(44, probe_types, rows))
+    expected = O.join_rows(b, p)
+    fused_ok = all(t != P.U128 for t in probe_types)
+    try:
+        for fused in (1, 0):
+            ctx.set_int("probe_fused", fused)
+            for scheme, bits, mat in (("phj-pure", [4, 3], 1), ("phj-pure", [5], 0), ("chj", None, -1)):
+                jo, fp, _ = run(ctx, scheme, b, p, bits, mat)
+                check(b, p, jo, fp)
+                names = {k["name"] for k in ctx.kernel_times()}
+                assert ("probe_fused" in names) == (fused == 1 and fused_ok), names
+    finally:
+        ctx.set_int("probe_fused", 1)
+
+
 @pytest.mark.parametrize("name", ["c2_mini", "c3_mini", "edge", "empty_probe", "empty_build", "no_match"])
 @pytest.mark.parametrize("chunk,budget", [(4096, 1), (1 << 24, 1), (1 << 24, 512)])
 def test_host_buffer_phj_bep(ctx, name, chunk, budget):
