@@ -181,6 +181,12 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        evict leaves round-robin (first pass 1..11 bits with at most 13
  *        bits below it, fewer than 2^32 probe rows; other joins take the
  *        batch form); 1 budget-sized probe batches;
+ *   "probe_fused": joins whose build keys are unique and whose build
+ *        payloads are packed (2+ columns of 1-8 bytes, 16 bytes in all; no
+ *        16-byte probe column): 1 (default) looks up and projects in one
+ *        kernel, the output sized by the probe rows and its rows placed in
+ *        reservation order; 0 looks up, scans and projects in two kernels.
+ *        Same output rows;
  *   "batch_graph": phj_batch_run's chain; 1 (default) replays it as a
  *        captured CUDA graph (one timing record, "batch_graph"), 0 launches
  *        it kernel by kernel at the batch's own sizes (a timing record per
