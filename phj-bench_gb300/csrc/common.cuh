@@ -165,6 +165,34 @@ struct Cols
     uint32_t n;
 };
 
+// Build payload columns packed row-major into 16 bytes: column c at byte
+// off[c] (widest first, so each offset is a multiple of its width; unused
+// bytes zero).
+struct PackSpec
+{
+    uint8_t off[kMaxCols];
+    uint32_t n;
+};
+
+// Row r of the payload columns `in`, packed.
+__device__ __forceinline__ uint4 pack_row(const Cols &in, uint64_t r, const PackSpec &pk)
+{
+    uint64_t h[2] = {0, 0};
+    for (uint32_t c = 0; c < in.n; ++c)
+    {
+        uint64_t v;
+        switch (in.width[c])
+        {
+            case 1: v = static_cast<const uint8_t *>(in.col[c])[r]; break;
+            case 2: v = static_cast<const uint16_t *>(in.col[c])[r]; break;
+            case 4: v = static_cast<const uint32_t *>(in.col[c])[r]; break;
+            default: v = static_cast<const uint64_t *>(in.col[c])[r]; break;
+        }
+        h[pk.off[c] >> 3] |= v << ((pk.off[c] & 7u) * 8u);
+    }
+    return make_uint4((uint32_t)h[0], (uint32_t)(h[0] >> 32), (uint32_t)h[1], (uint32_t)(h[1] >> 32));
+}
+
 // Copy element `src_i` of a column to element `dst_i` of another column of
 // the same width.
 __device__ __forceinline__ void copy_elem(void *dst, uint64_t dst_i, const void *src, uint64_t src_i, uint32_t w)

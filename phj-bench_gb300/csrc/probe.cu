@@ -852,27 +852,11 @@ __global__ void __launch_bounds__(kPNT, kProjMinBlocks) k_probe_project_window(c
     }
 }
 
-// Packs build payload columns row-major: row r's column c at byte off[c] of
-// the 16 bytes at out[r] (unused bytes zero).
-__global__ void k_pack_rows(const __grid_constant__ Cols in, uint64_t n, const __grid_constant__ PackedCols pk, uint4 * __restrict__ out)
+// Packs build payload columns row-major (pack_row) into out[r].
+__global__ void k_pack_rows(const __grid_constant__ Cols in, uint64_t n, const __grid_constant__ PackSpec pk, uint4 * __restrict__ out)
 {
     for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (uint64_t)gridDim.x * blockDim.x)
-    {
-        uint64_t h[2] = {0, 0};
-        for (uint32_t c = 0; c < in.n; ++c)
-        {
-            uint64_t v;
-            switch (in.width[c])
-            {
-                case 1: v = static_cast<const uint8_t *>(in.col[c])[r]; break;
-                case 2: v = static_cast<const uint16_t *>(in.col[c])[r]; break;
-                case 4: v = static_cast<const uint32_t *>(in.col[c])[r]; break;
-                default: v = static_cast<const uint64_t *>(in.col[c])[r]; break;
-            }
-            h[pk.off[c] >> 3] |= v << ((pk.off[c] & 7u) * 8u);
-        }
-        out[r] = make_uint4((uint32_t)h[0], (uint32_t)(h[0] >> 32), (uint32_t)h[1], (uint32_t)(h[1] >> 32));
-    }
+        out[r] = pack_row(in, r, pk);
 }
 
 // Chained duplicates (CHJ, leaves too large to group, lazily built BEP
@@ -1081,32 +1065,45 @@ uint64_t probe_lookup(phj_ctx * ctx, Scratch & s, const ProbeArgs & a_in, uint32
     return total;
 }
 
+// The packed layout of payload columns, when they pack: 2+ columns of 1-8
+// bytes, 16 bytes in all.
+static bool pack_spec_of(const Cols & payloads, PackSpec & pk)
+{
+    pk = PackSpec{};
+    if (payloads.n < 2)
+        return false;
+    // widest column first, so every offset is a multiple of its width
+    uint32_t order[kMaxCols];
+    for (uint32_t c = 0; c < payloads.n; ++c)
+        order[c] = c;
+    std::stable_sort(order, order + payloads.n, [&](uint32_t x, uint32_t y) { return payloads.width[x] > payloads.width[y]; });
+    uint32_t off = 0;
+    for (uint32_t i = 0; i < payloads.n; ++i)
+    {
+        const uint32_t c = order[i];
+        if (payloads.width[c] > 8)
+            return false;
+        pk.off[c] = (uint8_t)off;
+        off += payloads.width[c];
+    }
+    if (off > 16)
+        return false;
+    pk.n = payloads.n;
+    return true;
+}
+
 void pack_build_payloads(phj_ctx * ctx, Scratch & s, ProbeArgs & a, uint64_t build_rows)
 {
     a.packed = nullptr;
-    if (!ctx->pack_build || a.any_dup || a.build.n < 2 || build_rows == 0)
+    PackSpec pk;
+    if (!ctx->pack_build || a.any_dup || build_rows == 0 || !pack_spec_of(a.build, pk))
         return;
-    // widest column first, so every offset is a multiple of its width
-    uint32_t order[kMaxCols];
+    uint32_t bytes = 0;
     for (uint32_t c = 0; c < a.build.n; ++c)
-        order[c] = c;
-    std::stable_sort(order, order + a.build.n, [&](uint32_t x, uint32_t y) { return a.build.width[x] > a.build.width[y]; });
-    uint32_t off = 0;
-    PackedCols pk{};
-    for (uint32_t i = 0; i < a.build.n; ++i)
-    {
-        const uint32_t c = order[i];
-        if (a.build.width[c] > 8)
-            return;
-        pk.off[c] = (uint8_t)off;
-        off += a.build.width[c];
-    }
-    if (off > 16)
-        return;
-    pk.n = a.build.n;
+        bytes += a.build.width[c];
     uint4 * p = s.get<uint4>(build_rows);
     {
-        KTimer kt(ctx, "pack_build", build_rows, build_rows * (off + 16));
+        KTimer kt(ctx, "pack_build", build_rows, build_rows * (bytes + 16));
         // two CTAs per SM: the leaf-table build runs beside it
         k_pack_rows<<<(unsigned)std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(build_rows, 256), (uint64_t)ctx->num_sms * 2)), 256, 0, ctx->stream>>>(
             a.build, build_rows, pk, p);
