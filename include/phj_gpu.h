@@ -182,8 +182,9 @@ void *phj_ctx_stream(phj_ctx *ctx);
  *        bits below it, fewer than 2^32 probe rows; other joins take the
  *        batch form); 1 budget-sized probe batches;
  *   "probe_fused": joins whose build keys are unique and whose build
- *        payloads are packed (2+ columns of 1-8 bytes, 16 bytes in all; no
- *        16-byte probe column): 1 (default) looks up and projects in one
+ *        payloads are packed (2+ columns of 1-8 bytes, 16 bytes in all), one
+ *        column of 4 or 8 bytes, or none (and no 16-byte probe column): 1
+ *        (default) looks up and projects in one
  *        kernel, the output sized by the probe rows and its rows placed in
  *        reservation order; 0 looks up, scans and projects in two kernels.
  *        Same output rows;

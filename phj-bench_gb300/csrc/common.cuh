@@ -327,6 +327,15 @@ __device__ __forceinline__ void cp_async8(void * dst, const void * src, uint64_t
     asm volatile("cp.async.ca.shared.global.L2::cache_hint [%0], [%1], 8, %2;" ::"r"(smem_u32(dst)), "l"(src), "l"(pol) : "memory");
 }
 
+// 4- or 8-byte asynchronous copy from global to shared memory; dst and src
+// aligned to the size.
+template <int kBytes>
+__device__ __forceinline__ void cp_async_small(void * dst, const void * src)
+{
+    static_assert(kBytes == 4 || kBytes == 8, "cp.async.ca copies 4, 8 or 16 bytes");
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(dst)), "l"(src), "n"(kBytes) : "memory");
+}
+
 // 16-byte asynchronous copy from global to shared memory through L2 only;
 // dst and src 16-byte aligned.
 __device__ __forceinline__ void cp_async16(void * dst, const void * src)

@@ -23,6 +23,7 @@
 
 #include <cstdio>
 #include <cstdlib>
+#include <type_traits>
 
 namespace phjg
 {
@@ -662,18 +663,20 @@ __device__ __forceinline__ uint32_t fused_lookup(const ProbeArgs & a, uint64_t c
 constexpr uint32_t kFStage = 0, kFKeys = 2048, kFBrow = 4096, kFQueue = 5120, kFWarpBytes = 5632;
 
 // Lookup and projection in one pass, when no build key repeats and the
-// build payloads are packed.  A probe row then has at most one output row,
+// build payloads are packed (kGather 16: one 16-byte row of a.packed), or
+// are one column of 4 or 8 bytes (kGather 4 or 8: a.build.col[0]), or are
+// none (kGather 0).  A probe row then has at most one output row,
 // so the output is sized by the probe rows before the probe, and a warp
 // needs no offsets from other chunks: it looks its chunk up, reserves the
 // chunk's output rows with one atomic on the join's row counter, and
 // writes them -- no head array written and read back, no second read of
-// the probe keys.  Per half chunk, the build rows' 16-byte gathers go to
-// the warp's stage by asynchronous copies while the key column (from
+// the probe keys.  Per half chunk, the build rows' gathers go to the
+// warp's stage by asynchronous copies while the key column (from
 // shared memory) and the probe payload columns are written, then the build
 // payloads are written from the stage.  Warps take chunks by ticket (one
 // atomic a chunk).  A chunk's output rows are contiguous; chunks land in
 // reservation order.  pc holds the probe payload columns only.
-template <int kMode>
+template <int kMode, int kGather>
 __global__ void __launch_bounds__(kPNT, 3) k_probe_fused(const __grid_constant__ ProbeArgs a, const __grid_constant__ ProjCols pc,
                                                       const __grid_constant__ PackedCols bc, uint64_t * __restrict__ out_keys,
                                                       unsigned long long * __restrict__ out_rows, unsigned long long * __restrict__ tickets,
@@ -728,7 +731,10 @@ __global__ void __launch_bounds__(kPNT, 3) k_probe_fused(const __grid_constant__
                 if (brow[k] != kNoMatch)
                 {
                     one |= 1u << k;
-                    cp_async16(stage + k * 32 + lane, a.packed + brow[k]);
+                    if constexpr (kGather == 16)
+                        cp_async16(stage + k * 32 + lane, a.packed + brow[k]);
+                    else if constexpr (kGather != 0)
+                        cp_async_small<kGather>(stage + k * 32 + lane, static_cast<const uint8_t *>(a.build.col[0]) + (uint64_t)brow[k] * kGather);
                 }
             }
             uint32_t rel[kPH], running = 0;
@@ -746,8 +752,9 @@ __global__ void __launch_bounds__(kPNT, 3) k_probe_fused(const __grid_constant__
                 if (one >> u & 1u)
                     __stcs(out_keys + base + rel[u], key_s[i0 + (uint32_t)u * 32]);
             project_all<false>(pc, brow, prow, base, rel, one);
-            cp_async_wait_all();
+            if constexpr (kGather != 0)
             {
+                cp_async_wait_all();
                 uint4 row[kPH];
 #pragma unroll
                 for (int u = 0; u < kPH; ++u)
@@ -1148,14 +1155,30 @@ void probe_project(phj_ctx * ctx, const ProbeArgs & a, phj_output * out, uint64_
     dfree(ctx, b.flat);
 }
 
-// The fused probe: unique build keys with packed payloads, no 16-byte probe
-// payload column (its staged values would not fit the kernel's registers).
+// Bytes the one-pass probe gathers a build row: 16 (packed payloads), 4 or
+// 8 (one payload column of that width), 0 (no payload); -1: it does not
+// apply.
+static int fused_gather_bytes(const ProbeArgs & a)
+{
+    if (a.packed)
+        return 16;
+    if (a.build.n == 0)
+        return 0;
+    if (a.build.n == 1 && (a.build.width[0] == 4 || a.build.width[0] == 8))
+        return (int)a.build.width[0];
+    return -1;
+}
+
+// The fused probe: unique build keys whose payloads it gathers in one
+// piece, no 16-byte probe payload column (its staged values would not fit
+// the kernel's registers).
 static bool probe_fused_eligible(const phj_ctx * ctx, const ProbeArgs & a)
 {
     bool narrow = true;
     for (uint32_t c = 0; c < a.probe.n; ++c)
         narrow = narrow && a.probe.width[c] <= 8;
-    return ctx->probe_fused && narrow && !a.any_dup && a.packed && a.win_hi == 0 && a.probe_rows > 0 && a.probe_rows < (1ull << 32);
+    return ctx->probe_fused && narrow && !a.any_dup && fused_gather_bytes(a) >= 0 && a.win_hi == 0 && a.probe_rows > 0 &&
+           a.probe_rows < (1ull << 32);
 }
 
 // Unique build keys, packed build payloads: one pass that looks up and
@@ -1181,12 +1204,13 @@ static phj_output * probe_fused(phj_ctx * ctx, Scratch & s, const ProbeArgs & a,
             pc.width[pc.n] = a.probe.width[c];
             pc.by_build[pc.n++] = 0;
         }
+        const int gather = fused_gather_bytes(a);
         PackedCols bc{};
         for (uint32_t c = 0; c < a.build.n; ++c)
         {
             bc.dst[c] = o.left[c];
             bc.width[c] = (uint8_t)a.build.width[c];
-            bc.off[c] = a.packed_off[c];
+            bc.off[c] = gather == 16 ? a.packed_off[c] : 0; // one unpacked column sits at byte 0 of its stage slot
         }
         bc.n = a.build.n;
         auto launch = [&](auto kernel) {
@@ -1206,12 +1230,22 @@ static phj_output * probe_fused(phj_ctx * ctx, Scratch & s, const ProbeArgs & a,
         {
             KTimer kt(ctx, "probe_fused", a.probe_rows, 0);
             rec = kt.idx;
-            if (a.chj)
-                launch(k_probe_fused<kChj>);
-            else if (a.uniform_log2cap >= 0)
-                launch(k_probe_fused<kLeafUniform>);
-            else
-                launch(k_probe_fused<kLeafMeta>);
+            auto by_mode = [&](auto g) {
+                constexpr int kG = decltype(g)::value;
+                if (a.chj)
+                    launch(k_probe_fused<kChj, kG>);
+                else if (a.uniform_log2cap >= 0)
+                    launch(k_probe_fused<kLeafUniform, kG>);
+                else
+                    launch(k_probe_fused<kLeafMeta, kG>);
+            };
+            switch (gather)
+            {
+                case 16: by_mode(std::integral_constant<int, 16>{}); break;
+                case 8: by_mode(std::integral_constant<int, 8>{}); break;
+                case 4: by_mode(std::integral_constant<int, 4>{}); break;
+                default: by_mode(std::integral_constant<int, 0>{}); break;
+            }
             PHJ_LAUNCHED(ctx, "probe_fused");
         }
         unsigned long long total = 0;

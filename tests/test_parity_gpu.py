@@ -406,20 +406,24 @@ def test_packed_build_payloads(ctx, pack, build_types):
         ctx.set_int("pack_build", 1)
 
 
-@pytest.mark.parametrize("probe_types", [[P.U32], [P.U64, P.U16], [], [P.U128, P.U8]])
-def test_fused_probe_equals_split_and_oracle(ctx, probe_types):
-    # Unique build keys with packed payloads: the probe looks up and
-    # projects in one kernel (probe_fused 1, output rows in reservation
-    # order) or in two (0); both give the oracle's rows.  A 16-byte probe
-    # column keeps the two-kernel form.
-    bt = [P.U64, P.U32]
+@pytest.mark.parametrize("bt,probe_types", [([P.U64, P.U32], [P.U32]), ([P.U64, P.U32], [P.U64, P.U16]), ([P.U64, P.U32], []),
+                                            ([P.U64, P.U32], [P.U128, P.U8]), ([P.U64], [P.U32]), ([P.U32], [P.U64]),
+                                            ([], [P.U32]), ([P.U16], [P.U32]), ([P.U64, P.U64, P.U32], [P.U32])])
+def test_fused_probe_equals_split_and_oracle(ctx, bt, probe_types):
+    # Unique build keys whose payloads are packed, one 4- or 8-byte column,
+    # or none: the probe looks up and projects in one kernel (probe_fused 1,
+    # output rows in reservation order) or in two (0); both give the
+    # oracle's rows.  A 16-byte probe column, a 1- or 2-byte build column
+    # alone, or build columns that do not pack keep the two-kernel form.
     bk = G.gen_keys(0, 9000, 41, 11)
     b = P.BlockStream(bt, bk, G.payload_columns(42, bt, 9000))
     rows = 256 * 37 + 5
     p = P.BlockStream(probe_types, G.gen_keys(4, rows, 43, 11, domain=9000, match_permille=700),
                       G.payload_columns(44, probe_types, rows))
     expected = O.join_rows(b, p)
-    fused_ok = all(t != P.U128 for t in probe_types)
+    widths = [P.TYPE_WIDTH[t] for t in bt]
+    gathers = (len(bt) >= 2 and sum(widths) <= 16) or bt == [] or widths in ([4], [8])
+    fused_ok = gathers and all(t != P.U128 for t in probe_types)
     try:
         for fused in (1, 0):
             ctx.set_int("probe_fused", fused)
