@@ -42,12 +42,19 @@ def test_kernel_times_and_launch_count(ctx):
     b = ctx.generate(0, 100_000, 1, 2, [P.U64])
     p = ctx.generate(4, 400_000, 3, 2, [P.U32], domain=100_000, match_permille=900)
     n0 = ctx.launch_count()
-    out, res = ctx.run_phj_pure(b, p, [6, 6])
-    assert ctx.launch_count() > n0
-    names = [k["name"] for k in ctx.kernel_times()]
-    assert "probe_lookup" in names and "probe_project" in names and "build_scatter" in names
-    assert all(k["ms"] >= 0 for k in ctx.kernel_times())
-    fp = out.fingerprint()
     hb, hp = b.download(), p.download()
-    assert fp == O.join_fingerprint(hb, hp)
-    out.free(), b.free(), p.free()
+    # unique build keys with one 8-byte payload: the one-pass probe by
+    # default, the lookup and projection kernels with probe_fused 0
+    for fused, probe_kernels in ((1, ["probe_fused"]), (0, ["probe_lookup", "probe_project"])):
+        ctx.set_int("probe_fused", fused)
+        try:
+            out, res = ctx.run_phj_pure(b, p, [6, 6])
+        finally:
+            ctx.set_int("probe_fused", 1)
+        assert ctx.launch_count() > n0
+        names = [k["name"] for k in ctx.kernel_times()]
+        assert all(k in names for k in probe_kernels + ["build_scatter"]), names
+        assert all(k["ms"] >= 0 for k in ctx.kernel_times())
+        assert out.fingerprint() == O.join_fingerprint(hb, hp)
+        out.free()
+    b.free(), p.free()
