@@ -193,17 +193,32 @@ __device__ __forceinline__ T vload(const T * p)
 
 __device__ __forceinline__ uint64_t umin64(uint64_t x, uint64_t y) { return x < y ? x : y; }
 
-// Element src_i of a pool column (read through L2) to element dst_i of
-// another column of the same width.
+// Element src_i of a pool column (read through L2) to element dst_i of an
+// output column of the same width (a streaming store: output rows are not
+// read again, so they should not push pool pages and tables out of L2).
 __device__ __forceinline__ void copy_elem_cg(void * dst, uint64_t dst_i, const void * src, uint64_t src_i, uint32_t w)
 {
     switch (w)
     {
-        case 1: static_cast<uint8_t *>(dst)[dst_i] = (uint8_t)__ldcg(static_cast<const signed char *>(src) + src_i); break;
-        case 2: static_cast<uint16_t *>(dst)[dst_i] = __ldcg(static_cast<const unsigned short *>(src) + src_i); break;
-        case 4: static_cast<uint32_t *>(dst)[dst_i] = __ldcg(static_cast<const unsigned int *>(src) + src_i); break;
-        case 8: static_cast<unsigned long long *>(dst)[dst_i] = __ldcg(static_cast<const unsigned long long *>(src) + src_i); break;
-        default: static_cast<uint4 *>(dst)[dst_i] = __ldcg(static_cast<const uint4 *>(src) + src_i); break;
+        case 1: __stcs(static_cast<unsigned char *>(dst) + dst_i, (unsigned char)__ldcg(static_cast<const signed char *>(src) + src_i)); break;
+        case 2: __stcs(static_cast<unsigned short *>(dst) + dst_i, __ldcg(static_cast<const unsigned short *>(src) + src_i)); break;
+        case 4: __stcs(static_cast<unsigned int *>(dst) + dst_i, __ldcg(static_cast<const unsigned int *>(src) + src_i)); break;
+        case 8: __stcs(static_cast<unsigned long long *>(dst) + dst_i, __ldcg(static_cast<const unsigned long long *>(src) + src_i)); break;
+        default: __stcs(static_cast<uint4 *>(dst) + dst_i, __ldcg(static_cast<const uint4 *>(src) + src_i)); break;
+    }
+}
+
+// Element src_i of a build payload column (written before the launch) to
+// element dst_i of an output column, with a streaming store.
+__device__ __forceinline__ void copy_elem_out(void * dst, uint64_t dst_i, const void * src, uint64_t src_i, uint32_t w)
+{
+    switch (w)
+    {
+        case 1: __stcs(static_cast<unsigned char *>(dst) + dst_i, __ldg(static_cast<const unsigned char *>(src) + src_i)); break;
+        case 2: __stcs(static_cast<unsigned short *>(dst) + dst_i, __ldg(static_cast<const unsigned short *>(src) + src_i)); break;
+        case 4: __stcs(static_cast<unsigned int *>(dst) + dst_i, __ldg(static_cast<const unsigned int *>(src) + src_i)); break;
+        case 8: __stcs(static_cast<unsigned long long *>(dst) + dst_i, __ldg(static_cast<const unsigned long long *>(src) + src_i)); break;
+        default: __stcs(static_cast<uint4 *>(dst) + dst_i, __ldg(static_cast<const uint4 *>(src) + src_i)); break;
     }
 }
 
@@ -306,7 +321,7 @@ __device__ __forceinline__ void stage4(T * dst, const T * src, uint64_t r0, uint
     {
         const uint32_t i = i0 + u * kENT + threadIdx.x;
         if (i < n)
-            v[u] = kL2 ? __ldcg(src + r0 + i) : src[r0 + i];
+            v[u] = kL2 ? __ldcg(src + r0 + i) : __ldcs(src + r0 + i); // the input is read once
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u)
@@ -369,7 +384,7 @@ __device__ int scatter_tile(const EngineArgs & a, const Smem & sm, uint32_t g, u
         for (int u = 0; u < 4; ++u)
         {
             const uint32_t i = i0 + u * kENT + threadIdx.x;
-            k[u] = i < n ? a.pin.keys[r0 + i] : 0ull;
+            k[u] = i < n ? __ldcs(a.pin.keys + r0 + i) : 0ull;
         }
         for (uint32_t c = 0; c < a.pin.n; ++c)
             stage4_column<false>(sm.stage + a.col_off[c], a.pin.col[c], r0, i0, n, a.pin.width[c]);
@@ -1018,9 +1033,9 @@ __device__ void probe_rows_warp(const EngineArgs & a, const uint8_t * B, uint32_
             {
                 if (o < a.out_cap)
                 {
-                    a.out_keys[o] = key[k];
+                    __stcs(a.out_keys + o, (unsigned long long)key[k]);
                     for (uint32_t c = 0; c < a.bpart.n; ++c)
-                        copy_elem(a.out_l[c], o, a.bpart.col[c], b, a.bpart.width[c]);
+                        copy_elem_out(a.out_l[c], o, a.bpart.col[c], b, a.bpart.width[c]);
                     for (uint32_t c = 0; c < a.pin.n; ++c)
                         copy_elem_cg(a.out_r[c], o, B + a.col_off[c], i, a.pin.width[c]);
                 }
