@@ -376,8 +376,16 @@ BatchGraph & batch_workspace(phj_ctx * ctx, uint32_t n, uint64_t nq)
     W->o_carry = take(4ull * std::max<uint64_t>(scan_u32_carry(q_cap), 1));
     W->o_next = take(sizeof(unsigned int));
     W->bytes = at;
-    PHJ_CUDA(cudaMalloc(&W->dev, W->bytes));
-    PHJ_CUDA(cudaMallocHost(&W->host, W->o_cnt));
+    try
+    {
+        PHJ_CUDA(cudaMalloc(&W->dev, W->bytes));
+        PHJ_CUDA(cudaMallocHost(&W->host, W->o_cnt));
+    }
+    catch (...)
+    {
+        free_batch_graph(ctx); // no half-made workspace for the next call
+        throw;
+    }
     return *W;
 }
 

@@ -1250,6 +1250,8 @@ static phj_output * probe_fused(phj_ctx * ctx, Scratch & s, const ProbeArgs & a,
         }
         unsigned long long total = 0;
         read_small(ctx, {{&total, counter, sizeof(total)}});
+        if (total > out->cap)
+            throw Error(PHJ_ERR_CUDA, "internal: the one-pass probe counted more output rows than probe rows");
         out->rows = total;
         // algorithmic bytes: every probe row read, every output row written
         if (rec >= 0)
