@@ -436,6 +436,21 @@ def test_fused_probe_equals_split_and_oracle(ctx, bt, probe_types):
         ctx.set_int("probe_fused", 1)
 
 
+@pytest.mark.parametrize("rows,match", [(1, 1000), (255, 1000), (256, 0), (257, 500), (512 * 3 + 1, 1000)])
+def test_fused_probe_chunk_edges(ctx, rows, match):
+    # The one-pass probe at warp-chunk edges (256 rows a chunk): a single
+    # row, a chunk short by one, exactly one chunk with no match, one row
+    # past a chunk, all rows matching; with and without the probe side's
+    # written pass.
+    bt = [P.U64, P.U32]
+    b = P.BlockStream(bt, G.gen_keys(0, 3000, 71, 13), G.payload_columns(72, bt, 3000))
+    p = P.BlockStream([P.U64], G.gen_keys(4, rows, 73, 13, domain=3000, match_permille=match), G.payload_columns(74, [P.U64], rows))
+    for scheme, bits, mat in (("phj-pure", [3, 3], 1), ("phj-pure", [6], 0), ("chj", None, -1)):
+        jo, fp, _ = run(ctx, scheme, b, p, bits, mat)
+        check(b, p, jo, fp)
+        assert "probe_fused" in {k["name"] for k in ctx.kernel_times()}
+
+
 @pytest.mark.parametrize("name", ["c2_mini", "c3_mini", "edge", "empty_probe", "empty_build", "no_match"])
 @pytest.mark.parametrize("chunk,budget", [(4096, 1), (1 << 24, 1), (1 << 24, 512)])
 def test_host_buffer_phj_bep(ctx, name, chunk, budget):
