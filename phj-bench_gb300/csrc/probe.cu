@@ -19,6 +19,13 @@
 // This is the reference's "batchFind heads, expand chains into flat
 // (probe_idx, build_ref) arrays, then gather column-major" with the head
 // array in memory and the expansion folded into the projection.
+//
+// When no build key repeats (a probe row then has at most one output row)
+// and the build payloads are gathered in one piece, one kernel does both:
+//   k_probe_fused    per warp chunk (taken by ticket): the lookups, one
+//                    reservation of the chunk's output rows on the join's
+//                    row counter, then the projection from shared memory;
+//                    the output is sized by the probe rows beforehand.
 #include "internal.h"
 
 #include <cstdio>
@@ -658,8 +665,7 @@ __device__ __forceinline__ uint32_t fused_lookup(const ProbeArgs & a, uint64_t c
 // Shared memory of one warp of the fused kernel: the build rows' gather
 // stage (half a chunk of 16-byte rows), the chunk's keys, head build rows
 // and queue; 44 KB a CTA, static, so three CTAs a SM leave L1 about 120 KB
-// (a 60 KB layout that also staged a probe payload column left about 70 KB
-// and ran 4.7 ms against 3.9 on 16M x 256M).
+// (16 KB more a CTA ran the 16M x 256M probe 5% slower).
 constexpr uint32_t kFStage = 0, kFKeys = 2048, kFBrow = 4096, kFQueue = 5120, kFWarpBytes = 5632;
 
 // Lookup and projection in one pass, when no build key repeats and the
