@@ -339,8 +339,10 @@ phj_status phj_run_phj_bep_host(phj_ctx *ctx, const phj_block_stream *build, con
  * of its row counts reads nothing back to the host; it is captured into a
  * CUDA graph on the first call and replayed by later calls whose batch fits
  * the context's workspace (it grows, and the chain is captured again, for a
- * larger batch; option "batch_graph").  The call synchronizes the context's
- * stream. */
+ * larger batch; option "batch_graph").  The workspace (a few MiB: the
+ * joins' descriptors and the partitions' counts and offsets) lives until
+ * phj_ctx_destroy and is not counted in peak_mem_bytes.  The call
+ * synchronizes the context's stream. */
 phj_status phj_batch_run(phj_ctx *ctx, uint32_t n, const phj_table *const *builds, const phj_table *const *probes,
                          phj_output **outs, phj_batch_result *result);
 
